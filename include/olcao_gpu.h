@@ -1,0 +1,204 @@
+/*
+ * olcao_gpu.h -- C ABI of the GB300 implementation of OLCAO's per-SCF-iteration
+ * hot path: Gaussian two/three-centre integrals, their Bloch sums into
+ * H(k)/S(k), the valence-core orthogonalisation, the upper-packed integral
+ * layout, Hamiltonian assembly and the per-k complex Hermitian generalised
+ * eigen-solve.
+ *
+ * Every entry point takes plain pointers and sizes.  Arrays are column-major
+ * (Fortran order) and complex numbers are interleaved (re, im) binary64, so a
+ * Fortran caller passes its own arrays through ISO_C_BINDING unchanged.
+ * Host pointers are copied in; "device" pointers must live on the context's
+ * device.  Status 0 means success; any other value is an olc_status_t and
+ * olc_last_error() returns the message.
+ *
+ * Reference interfaces replaced (paths within UMKC-CPG/olcao):
+ *   olc_create                 setupSCF set-up: initializeLattice,
+ *                              initializeFindVec, computePhaseFactors,
+ *                              renormalizeBasis, makeAlpha*Dist
+ *                              (src/olcao/OLCAO_Setup.f90:88-126,
+ *                               src/olcao/lattice.f90:300-432,
+ *                               src/olcao/kpoints.f90:286-310,
+ *                               src/olcao/basis.f90:55-243,
+ *                               src/olcao/gaussRelations.f90:64-278)
+ *   olc_gauss_overlap          gaussOverlapOL / KE / NP / EP (+ saveCurrentPair)
+ *                              (src/olcao/integrals.F90:81-486, 490-900,
+ *                               1324-1715, 1719-2122;
+ *                               src/olcao/intgSaving.F90:56-550)
+ *   olc_ortho_pack             orthoOL / ortho(opCode) + makeValeVale packing
+ *                              (src/olcao/integrals.F90:2601-2853,
+ *                               src/olcao/intgOrtho.F90:23-187)
+ *   olc_assemble_hamiltonian   readPackedMatrix(Accum) + unpackMatrix
+ *                              (src/olcao/secularEqn.F90:128-166,
+ *                               src/olcao/matrixSubs.F90:248-355)
+ *   olc_solve_zhegv            solveZHEGV (src/olcao/interfaces.F90:73-120)
+ *   olc_scf_iteration          one pass of secularEqnAllKP with the
+ *                              potential-dependent integrals recomputed
+ *                              (src/olcao/secularEqn.F90:33-287,
+ *                               src/uolcao/integrals.F90:2860-3605 fused form)
+ */
+#ifndef OLCAO_GPU_H
+#define OLCAO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OLC_MAX_ALPHAS      32   /* atomic Gaussian exponents per atom type  */
+#define OLC_MAX_RADIAL      12   /* radial functions per atom type           */
+#define OLC_MAX_POT_ALPHAS  32   /* potential Gaussian exponents per type    */
+#define OLC_MAX_STATES      40   /* basis states (l,m) per atom type         */
+
+typedef enum {
+  OLC_OK = 0,
+  OLC_ERR_ARG = 1,            /* invalid argument / inconsistent sizes       */
+  OLC_ERR_CUDA = 2,           /* CUDA runtime or library failure             */
+  OLC_ERR_LATTICE = 3,        /* "More lattice points needed" (integrals.F90:249-255) */
+  OLC_ERR_NOT_PD = 4,         /* S(k) not positive definite: ZHEGV info > n   */
+  OLC_ERR_EIGEN = 5,          /* eigen-solver failed to converge: 0 < info <= n */
+  OLC_ERR_ALLOC = 6,          /* device allocation failed                    */
+  OLC_ERR_UNSUPPORTED = 7     /* feature outside this build (e.g. l > 3)     */
+} olc_status_t;
+
+/* One atom type (reference: atomTypes(i), src/olcao/atomicTypes.f90:40-120).
+ * Radial functions are listed valence first, then core; coefficient arrays
+ * hold numOrbAlphas(l+1) leading entries, the rest must be zero. */
+typedef struct {
+  int32_t element;                        /* element id, 1-based              */
+  int32_t num_orb_alphas[4];              /* numOrbAlphas(1..4): s >= p >= d >= f */
+  double  alphas[OLC_MAX_ALPHAS];         /* ascending                         */
+  int32_t num_vale_radial;
+  int32_t num_core_radial;
+  int32_t radial_l[OLC_MAX_RADIAL];
+  double  radial_coeff[OLC_MAX_RADIAL][OLC_MAX_ALPHAS];
+} olc_atom_type_t;
+
+/* One potential type (reference: potTypes(i), src/olcao/potTypes.f90:20-75). */
+typedef struct {
+  int32_t element;
+  int32_t num_alphas;
+  double  nuc_charge;                     /* Z, the nuclear factor            */
+  double  nuc_alpha;                      /* Gaussian nuclear exponent        */
+  double  alphas[OLC_MAX_POT_ALPHAS];     /* ascending                         */
+} olc_pot_type_t;
+
+/* Whole-system description.  All positions and vectors are in bohr.
+ * real_vectors is realVectors(xyz, abc) column-major (column = a, b, c).
+ * Potential sites of one type must be consecutive (the reference's
+ * currPotNumber..+multiplicity-1 convention, integrals.F90:2527-2530). */
+typedef struct {
+  double real_vectors[9];
+  int32_t num_atom_types;
+  const olc_atom_type_t* atom_types;
+  int32_t num_atom_sites;
+  const int32_t* site_type;               /* [num_atom_sites], 0-based        */
+  const double*  site_pos;                /* [3*num_atom_sites]               */
+  int32_t num_pot_types;
+  const olc_pot_type_t* pot_types;
+  int32_t num_pot_sites;
+  const int32_t* pot_site_type;           /* [num_pot_sites], 0-based         */
+  const double*  pot_site_pos;            /* [3*num_pot_sites]                */
+  int32_t num_kpoints;
+  const double*  kpoints_abc;             /* [3*num_kpoints] fractional       */
+  double basis_fn_thresh;                 /* BASIS_FN convergence, e.g. 1e-16 */
+} olc_system_t;
+
+/* Integral operators (the reference's opCode values, integrals.F90:2710-2853). */
+typedef enum {
+  OLC_OP_OVERLAP = 1,     /* gaussOverlapOL -> atomOverlap                    */
+  OLC_OP_KINETIC = 2,     /* gaussOverlapKE -> atomKEOverlap                  */
+  OLC_OP_NUCLEAR = 3,     /* gaussOverlapNP -> atomNucOverlap                 */
+  OLC_OP_ELECPOT = 4,     /* gaussOverlapEP -> atomPotOverlap(term)           */
+  OLC_OP_HAMILTONIAN = 6  /* KE + NP + sum_j c_j V_j in one pass (fused form) */
+} olc_op_t;
+
+typedef enum {
+  OLC_PREC_FP64 = 0,      /* plain FP64 path                                  */
+  OLC_PREC_MIXED = 1      /* FP32 far-shell terms, FP64 near-shell and Boys   */
+} olc_precision_t;
+
+typedef struct olc_context olc_context_t;
+
+/* Sizes derived by olc_create (valeDim, coreDim, potDim, numKPoints, ...). */
+typedef struct {
+  int32_t vale_dim;
+  int32_t core_dim;
+  int32_t pot_dim;
+  int32_t num_kpoints;
+  int32_t num_cells;          /* numCellsReal                                 */
+  int32_t num_pair_tasks;     /* surviving (atom pair, lattice cell) blocks    */
+  int64_t packed_len;         /* vale_dim*(vale_dim+1)/2                       */
+} olc_dims_t;
+
+/* Library version and last error of the calling thread. */
+const char* olc_version(void);
+int olc_last_error(char* buf, size_t len);
+
+/* Set-up: copies the system to the device and builds the lattice, k-point
+ * phases, basis and screening tables.  stream may be NULL (legacy stream) or
+ * a cudaStream_t the caller owns; all work of this context runs on it. */
+int olc_create(const olc_system_t* sys, void* stream, olc_context_t** ctx);
+int olc_destroy(olc_context_t* ctx);
+int olc_get_dims(const olc_context_t* ctx, olc_dims_t* dims);
+int olc_set_stream(olc_context_t* ctx, void* stream);
+
+/* One integral pass for operator op (term = potential term index for
+ * OLC_OP_ELECPOT, 0-based; coeffs[pot_dim] for OLC_OP_HAMILTONIAN, else NULL).
+ * Writes the un-orthogonalised blocks saveCurrentPair produces, for all k:
+ *   vv[vale_dim, vale_dim, nk] (upper triangle meaningful),
+ *   cv[core_dim, vale_dim, nk], cc[core_dim, core_dim, nk]
+ * as DEVICE complex128 arrays (any of cv/cc may be NULL when core_dim == 0). */
+int olc_gauss_overlap(olc_context_t* ctx, int op, int term,
+                      const double* coeffs, int precision,
+                      double* vv, double* cv, double* cc);
+
+/* Orthogonalise and pack, for all k (DEVICE arrays).  For the overlap
+ * operator pass cv == s_cv.  Outputs packed[2, packed_len, nk] with the
+ * reference's |x| < 1e-10 flush when core_dim > 0. vv is overwritten. */
+int olc_ortho_pack(olc_context_t* ctx, int is_overlap, double* vv,
+                   const double* cv, const double* cc, const double* s_cv,
+                   double* packed);
+
+/* H(k) packed = NP + KE + sum_j c_j V_j with the reference's rule that a
+ * zero coefficient adds the term with factor 1 (matrixSubs.F90:278-282).
+ * terms[nterm] are DEVICE pointers to packed[2, packed_len, nk] arrays. */
+int olc_assemble_hamiltonian(olc_context_t* ctx, const double* const* terms,
+                             const double* coeffs, int nterm, double* packed_h);
+
+/* Generalised eigen-problem for every k: A x = lambda B x with A, B given
+ * upper-packed (DEVICE).  Writes eigenvalues[num_states, nk] (Hartree,
+ * ascending) and, if vectors != NULL, vectors[vale_dim, num_states, nk]
+ * complex128.  info[nk] receives LAPACK-style info codes (host memory). */
+int olc_solve_zhegv(olc_context_t* ctx, const double* packed_h,
+                    const double* packed_s, int num_states,
+                    double* eigenvalues, double* vectors, int32_t* info);
+
+/* Set-up of the iteration-invariant parts of the SCF pass: S(k) orthogonalised
+ * and factored, and H0 = ortho(KE + NP).  Must precede olc_scf_iteration. */
+int olc_scf_prepare(olc_context_t* ctx, int precision);
+
+/* One SCF-iteration pass of the hot path: V = sum_j c_j V_j recomputed from
+ * the integrals with the given coefficients, orthogonalised, added to H0,
+ * and the generalised eigen-problem solved for all k.  coeffs is a HOST
+ * array [pot_dim]; eigenvalues is a HOST or DEVICE array [num_states, nk]
+ * (eig_on_device selects).  vectors (DEVICE, may be NULL) as above. */
+int olc_scf_iteration(olc_context_t* ctx, const double* coeffs, int precision,
+                      int num_states, double* eigenvalues, int eig_on_device,
+                      double* vectors);
+
+/* Primitive-level entry (testing and integration checks): one call of the
+ * generated primitives (gaussIntegrals.f90) for a batch of inputs on the
+ * device.  kind: 1 overlap2CIntg, 2 kinetic2CIntg, 3 nuclear3CIntg,
+ * 4 electron3CIntg.  in[n*12] = (a1,a2,a3,Ax,Ay,Az,Bx,By,Bz,Cx,Cy,Cz),
+ * lmalpha[n*2]; out[n*256] = sh(16,16) column-major (host arrays). */
+int olc_primitive_batch(int kind, int n, const double* in,
+                        const int32_t* lmalpha, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OLCAO_GPU_H */

@@ -1,0 +1,229 @@
+"""Python front end of libolcao_gb300 (C ABI in include/olcao_gpu.h).
+
+Mirrors the reference's module procedures for the hot path:
+
+=========================  ==================================================
+this module                reference (src/olcao/...)
+=========================  ==================================================
+``Context(system)``        setupSCF set-up: initializeLattice, computePhase-
+                           Factors, renormalizeBasis, makeAlpha*Dist
+``gauss_overlap(OL)``      gaussOverlapOL     integrals.F90:81-486
+``gauss_overlap(KE)``      gaussOverlapKE     integrals.F90:490-900
+``gauss_overlap(NP)``      gaussOverlapNP     integrals.F90:1324-1715
+``gauss_overlap(EP, j)``   gaussOverlapEP     integrals.F90:1719-2122
+``ortho_pack``             orthoOL / ortho    integrals.F90:2601-2853
+``assemble_hamiltonian``   secularEqn H build secularEqn.F90:128-166
+``solve_zhegv``            solveZHEGV         interfaces.F90:73-120
+``scf_iteration``          secularEqnAllKP with the potential-dependent
+                           integrals recomputed (fused form)
+=========================  ==================================================
+
+Device buffers are torch CUDA tensors (torch is only the allocator and
+stream provider).  There is no CPU fallback: when the compiled library is
+missing every call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libolcao_gb300.so")
+
+OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT, OP_HAMILTONIAN = 1, 2, 3, 4, 6
+PREC_FP64, PREC_MIXED = 0, 1
+
+EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
+           "olc_get_dims", "olc_set_stream", "olc_gauss_overlap",
+           "olc_ortho_pack", "olc_assemble_hamiltonian", "olc_solve_zhegv",
+           "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch")
+
+_LIB: Optional[C.CDLL] = None
+
+
+class OlcError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"olcao_gb300 status {status}: {msg}")
+        self.status = status
+
+
+class Dims(C.Structure):
+    _fields_ = [("vale_dim", C.c_int32), ("core_dim", C.c_int32),
+                ("pot_dim", C.c_int32), ("num_kpoints", C.c_int32),
+                ("num_cells", C.c_int32), ("num_pair_tasks", C.c_int32),
+                ("packed_len", C.c_int64)]
+
+
+def lib() -> C.CDLL:
+    """Load the compiled library; raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise OlcError(-1, f"{LIB_PATH} is missing: run olcao_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, i32, dp = C.c_void_p, C.c_int, C.c_void_p
+        L.olc_version.restype = C.c_char_p
+        L.olc_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        L.olc_create.argtypes = [vp, vp, C.POINTER(vp)]
+        L.olc_destroy.argtypes = [vp]
+        L.olc_get_dims.argtypes = [vp, C.POINTER(Dims)]
+        L.olc_set_stream.argtypes = [vp, vp]
+        L.olc_gauss_overlap.argtypes = [vp, i32, i32, dp, i32, dp, dp, dp]
+        L.olc_ortho_pack.argtypes = [vp, i32, dp, dp, dp, dp, dp]
+        L.olc_assemble_hamiltonian.argtypes = [vp, dp, dp, i32, dp]
+        L.olc_solve_zhegv.argtypes = [vp, dp, dp, i32, dp, dp, dp]
+        L.olc_scf_prepare.argtypes = [vp, i32]
+        L.olc_scf_iteration.argtypes = [vp, dp, i32, i32, dp, i32, dp]
+        L.olc_primitive_batch.argtypes = [i32, i32, dp, dp, dp]
+        for name in EXPORTS[2:]:
+            getattr(L, name).restype = C.c_int
+        _LIB = L
+    return _LIB
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    lib().olc_last_error(buf, 1024)
+    return buf.value.decode()
+
+
+def _check(status: int):
+    if status != 0:
+        raise OlcError(status, last_error())
+
+
+def _ptr(t) -> Optional[int]:
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+def primitive_batch(kind: int, params: np.ndarray, lmalpha: np.ndarray) -> np.ndarray:
+    """Evaluate primitive sh(16,16) blocks on the device (kind 1 overlap,
+    2 kinetic, 3 nuclear, 4 electron 3-centre); returns [n, 16, 16] indexed
+    [item, row lm1, col lm2]."""
+    p = np.ascontiguousarray(params, np.float64)
+    lm = np.ascontiguousarray(lmalpha, np.int32)
+    n = p.shape[0]
+    out = np.zeros((n, 256))
+    _check(lib().olc_primitive_batch(kind, n, p.ctypes.data, lm.ctypes.data, out.ctypes.data))
+    return out.reshape(n, 16, 16).transpose(0, 2, 1)
+
+
+class Context:
+    """One system on the current CUDA device (olc_create)."""
+
+    def __init__(self, system, stream=None):
+        import torch
+        self.torch = torch
+        self.system = system
+        self._struct = system.to_struct()
+        h = C.c_void_p()
+        s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _check(lib().olc_create(C.byref(self._struct), C.c_void_p(s), C.byref(h)))
+        self.h = h
+        d = Dims()
+        _check(lib().olc_get_dims(h, C.byref(d)))
+        self.vale_dim, self.core_dim = d.vale_dim, d.core_dim
+        self.pot_dim, self.nk = d.pot_dim, d.num_kpoints
+        self.num_cells, self.num_pair_tasks = d.num_cells, d.num_pair_tasks
+        self.packed_len = d.packed_len
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().olc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        _check(lib().olc_set_stream(self.h, C.c_void_p(stream.cuda_stream)))
+
+    # -- buffers ---------------------------------------------------------------
+    def _z(self, *shape):
+        return self.torch.zeros(*shape, dtype=self.torch.complex128, device="cuda")
+
+    def blocks(self):
+        nv, nc, nk = self.vale_dim, self.core_dim, self.nk
+        vv = self._z(nk, nv, nv)
+        cv = self._z(nk, nv, nc) if nc else None
+        cc = self._z(nk, nc, nc) if nc else None
+        return vv, cv, cc
+
+    # -- reference module procedures ------------------------------------------
+    def gauss_overlap(self, op: int, term: int = 0, coeffs=None,
+                      precision: int = PREC_FP64, out=None):
+        """One integral pass; returns (vv, cv, cc) device tensors shaped
+        [nk, cols, rows] (the reference's column-major (rows, cols, nk))."""
+        vv, cv, cc = out if out is not None else self.blocks()
+        cptr = None
+        if coeffs is not None:
+            carr = np.ascontiguousarray(coeffs, np.float64)
+            cptr = carr.ctypes.data
+        _check(lib().olc_gauss_overlap(self.h, op, term, cptr, precision, _ptr(vv),
+                                       _ptr(cv), _ptr(cc)))
+        return vv, cv, cc
+
+    def ortho_pack(self, is_overlap: bool, vv, cv, cc, scv):
+        packed = self.torch.zeros(self.nk, self.packed_len, 2, dtype=self.torch.float64,
+                                  device="cuda")
+        _check(lib().olc_ortho_pack(self.h, int(is_overlap), _ptr(vv), _ptr(cv), _ptr(cc),
+                                    _ptr(scv), _ptr(packed)))
+        return packed
+
+    def packed_operators(self, terms: Optional[Sequence[int]] = None) -> Dict[str, object]:
+        """OLCAOsetup's stored integrals: packed, orthogonalised S, KE, NP, V_j."""
+        vvS, cvS, ccS = self.gauss_overlap(OP_OVERLAP)
+        out = {"S": self.ortho_pack(True, vvS.clone(), cvS, ccS, cvS)}
+        for name, op in (("KE", OP_KINETIC), ("NP", OP_NUCLEAR)):
+            vv, cv, cc = self.gauss_overlap(op)
+            out[name] = self.ortho_pack(False, vv, cv, cc, cvS)
+        terms = range(self.pot_dim) if terms is None else terms
+        for j in terms:
+            vv, cv, cc = self.gauss_overlap(OP_ELECPOT, j)
+            out[f"V{j}"] = self.ortho_pack(False, vv, cv, cc, cvS)
+        return out
+
+    def assemble_hamiltonian(self, packed: Dict[str, object], coeffs) -> object:
+        terms = [packed["NP"], packed["KE"]] + [packed[f"V{j}"] for j in range(self.pot_dim)]
+        co = np.concatenate([[1.0, 1.0], np.asarray(coeffs, np.float64)])
+        ptrs = (C.c_void_p * len(terms))(*[t.data_ptr() for t in terms])
+        out = self.torch.empty_like(packed["NP"])
+        _check(lib().olc_assemble_hamiltonian(self.h, C.cast(ptrs, C.c_void_p),
+                                              co.ctypes.data, len(terms), out.data_ptr()))
+        return out
+
+    def solve_zhegv(self, packed_h, packed_s, num_states: int, vectors: bool = False):
+        torch = self.torch
+        eig = torch.zeros(self.nk, num_states, dtype=torch.float64, device="cuda")
+        vec = (torch.zeros(self.nk, num_states, self.vale_dim, dtype=torch.complex128,
+                           device="cuda") if vectors else None)
+        info = np.zeros(self.nk, np.int32)
+        _check(lib().olc_solve_zhegv(self.h, packed_h.data_ptr(), packed_s.data_ptr(),
+                                     num_states, eig.data_ptr(), _ptr(vec), info.ctypes.data))
+        return eig, vec, info
+
+    def scf_prepare(self, precision: int = PREC_FP64):
+        _check(lib().olc_scf_prepare(self.h, precision))
+
+    def scf_iteration(self, coeffs, num_states: int, precision: int = PREC_FP64,
+                      eig_out=None, vectors=None):
+        """One SCF pass; returns eigenvalues [nk, num_states].  eig_out may be
+        a host numpy array or a device tensor."""
+        co = np.ascontiguousarray(coeffs, np.float64)
+        if eig_out is None:
+            eig_out = np.zeros((self.nk, num_states))
+        on_dev = 0 if isinstance(eig_out, np.ndarray) else 1
+        _check(lib().olc_scf_iteration(self.h, co.ctypes.data, precision, num_states,
+                                       _ptr(eig_out), on_dev, _ptr(vectors)))
+        return eig_out

@@ -1,0 +1,172 @@
+// C ABI of libolcao_gb300 (declared in include/olcao_gpu.h).
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "olc_common.h"
+
+namespace olc {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return OLC_OK;
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? OLC_ERR_ALLOC : OLC_ERR_CUDA;
+}
+
+int build_phase_table(olc_context* ctx);
+int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const double* cv,
+                  const double* cc, const double* scv, double* packed, double* full,
+                  const double* add);
+
+}  // namespace olc
+
+using namespace olc;
+
+extern "C" {
+
+const char* olc_version(void) { return "olcao_gb300 0.1 (sm_103a)"; }
+
+int olc_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return OLC_ERR_ARG;
+  std::snprintf(buf, len, "%s", g_last_error.c_str());
+  return OLC_OK;
+}
+
+int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
+  if (!out) return fail(OLC_ERR_ARG, "olc_create: null output");
+  *out = nullptr;
+  int dev = 0;
+  int st = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st) return st;
+  olc_context* ctx = new olc_context();
+  ctx->device = dev;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  if (cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) {
+    delete ctx;
+    return fail(OLC_ERR_CUDA, "cublasCreate failed");
+  }
+  if (cusolverDnCreate(&ctx->solver) != CUSOLVER_STATUS_SUCCESS) {
+    cublasDestroy(ctx->blas);
+    delete ctx;
+    return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
+  }
+  cublasSetStream(ctx->blas, ctx->stream);
+  cusolverDnSetStream(ctx->solver, ctx->stream);
+  st = build_system(ctx, sys);
+  if (!st) st = build_phase_table(ctx);
+  if (!st) st = cuda_check(cudaStreamSynchronize(ctx->stream), "olc_create sync");
+  if (st) {
+    std::string keep = g_last_error;
+    olc_destroy(ctx);
+    g_last_error = keep;
+    return st;
+  }
+  *out = ctx;
+  return OLC_OK;
+}
+
+int olc_destroy(olc_context_t* ctx) {
+  if (!ctx) return OLC_OK;
+  cudaStreamSynchronize(ctx->stream);
+  for (void* p : ctx->allocations) cudaFree(p);
+  for (int c = 0; c < kNumClasses; ++c) (void)c;
+  if (ctx->d_solver_work) cudaFree(ctx->d_solver_work);
+  if (ctx->blas) cublasDestroy(ctx->blas);
+  if (ctx->solver) cusolverDnDestroy(ctx->solver);
+  delete ctx;
+  return OLC_OK;
+}
+
+int olc_get_dims(const olc_context_t* ctx, olc_dims_t* dims) {
+  if (!ctx || !dims) return fail(OLC_ERR_ARG, "olc_get_dims: null argument");
+  *dims = ctx->dims;
+  return OLC_OK;
+}
+
+int olc_set_stream(olc_context_t* ctx, void* stream) {
+  if (!ctx) return fail(OLC_ERR_ARG, "olc_set_stream: null context");
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  cublasSetStream(ctx->blas, ctx->stream);
+  cusolverDnSetStream(ctx->solver, ctx->stream);
+  return OLC_OK;
+}
+
+int olc_gauss_overlap(olc_context_t* ctx, int op, int term, const double* coeffs, int precision,
+                      double* vv, double* cv, double* cc) {
+  if (!ctx || !vv) return fail(OLC_ERR_ARG, "olc_gauss_overlap: null argument");
+  int st;
+  if (op == OLC_OP_HAMILTONIAN) {
+    if (!coeffs) return fail(OLC_ERR_ARG, "OLC_OP_HAMILTONIAN needs coefficients");
+    const int pd = ctx->dims.pot_dim;
+    std::vector<double> c(coeffs, coeffs + pd);
+    double* dco = nullptr;
+    if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * std::max(1, pd), ctx->stream), "malloc"))) return st;
+    cudaMemcpyAsync(dco, c.data(), sizeof(double) * pd, cudaMemcpyHostToDevice, ctx->stream);
+    st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, precision, false);
+    if (!st) st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, precision, true);
+    if (!st) st = run_primitives(ctx, OLC_OP_ELECPOT, 0, dco, precision, true);
+    cudaFreeAsync(dco, ctx->stream);
+  } else if (op >= OLC_OP_OVERLAP && op <= OLC_OP_ELECPOT) {
+    if (op == OLC_OP_ELECPOT && (term < 0 || term >= ctx->dims.pot_dim))
+      return fail(OLC_ERR_ARG, "potential term out of range");
+    st = run_primitives(ctx, op, term, nullptr, precision, false);
+  } else {
+    return fail(OLC_ERR_ARG, "unknown operator");
+  }
+  if (st) return st;
+  st = run_contract_bloch(ctx, vv, cv, cc);
+  if (st) return st;
+  return cuda_check(cudaStreamSynchronize(ctx->stream), "olc_gauss_overlap sync");
+}
+
+int olc_ortho_pack(olc_context_t* ctx, int is_overlap, double* vv, const double* cv,
+                   const double* cc, const double* s_cv, double* packed) {
+  if (!ctx || !vv || !packed) return fail(OLC_ERR_ARG, "olc_ortho_pack: null argument");
+  if (ctx->dims.core_dim && (!cv || !cc || !s_cv))
+    return fail(OLC_ERR_ARG, "olc_ortho_pack: core blocks required");
+  int st = ortho_pack_ex(ctx, is_overlap != 0, vv, cv, cc, is_overlap ? cv : s_cv, packed,
+                         nullptr, nullptr);
+  if (st) return st;
+  return cuda_check(cudaStreamSynchronize(ctx->stream), "olc_ortho_pack sync");
+}
+
+int olc_assemble_hamiltonian(olc_context_t* ctx, const double* const* terms, const double* coeffs,
+                             int nterm, double* packed_h) {
+  if (!ctx || !terms || !coeffs || !packed_h) return fail(OLC_ERR_ARG, "olc_assemble_hamiltonian: null argument");
+  return assemble_packed(ctx, terms, coeffs, nterm, packed_h);
+}
+
+int olc_solve_zhegv(olc_context_t* ctx, const double* packed_h, const double* packed_s,
+                    int num_states, double* eigenvalues, double* vectors, int32_t* info) {
+  if (!ctx || !packed_h || !packed_s || !eigenvalues) return fail(OLC_ERR_ARG, "olc_solve_zhegv: null argument");
+  return solve_packed(ctx, packed_h, packed_s, num_states, eigenvalues, vectors, info);
+}
+
+int olc_scf_prepare(olc_context_t* ctx, int precision) {
+  if (!ctx) return fail(OLC_ERR_ARG, "olc_scf_prepare: null context");
+  return scf_prepare(ctx, precision);
+}
+
+int olc_scf_iteration(olc_context_t* ctx, const double* coeffs, int precision, int num_states,
+                      double* eigenvalues, int eig_on_device, double* vectors) {
+  if (!ctx || !coeffs || !eigenvalues) return fail(OLC_ERR_ARG, "olc_scf_iteration: null argument");
+  return scf_iteration(ctx, coeffs, precision, num_states, eigenvalues, eig_on_device, vectors);
+}
+
+int olc_primitive_batch(int kind, int n, const double* in, const int32_t* lmalpha, double* out) {
+  if (n > 0 && (!in || !lmalpha || !out)) return fail(OLC_ERR_ARG, "olc_primitive_batch: null argument");
+  return primitive_batch_device(kind, n, in, lmalpha, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,179 @@
+// Internal declarations shared by the host set-up, the integral kernels and the
+// dense linear-algebra stages of libolcao_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "olcao_gpu.h"
+
+namespace olc {
+
+constexpr double kPi = 3.141592653589793;
+constexpr int kMaxL = 2;            // highest l the integral kernels are built for
+constexpr int kMaxLm = 9;           // (kMaxL+1)^2 real harmonics s..d
+constexpr int kNumClasses = (kMaxL + 1) * (kMaxL + 1);
+
+// Per-atom-type data the kernels read (basis.f90:55-243 restated).
+struct DevType {
+  int32_t element;      // 0-based element id
+  int32_t nalpha;       // numOrbAlphas(1)
+  int32_t nstates;      // valence + core states
+  int32_t nvale;
+  int32_t ncore;
+  int32_t lmax_alpha[OLC_MAX_ALPHAS];   // l range available at each exponent
+  int32_t lm_index[OLC_MAX_STATES];     // 1-based lm of each state
+  double alphas[OLC_MAX_ALPHAS];
+  double basis[OLC_MAX_ALPHAS * OLC_MAX_STATES];   // [alpha][state]
+};
+
+// One surviving atom pair (i <= j) with its nearest-image lattice vector.
+struct DevPair {
+  int32_t i, j;
+  int32_t task_begin, task_end;   // its (pair, cell) tasks
+  double L[3];
+};
+
+// One (pair, cell) block.
+struct DevTask {
+  int32_t pair;
+  int32_t cell;
+  double sep;                    // |A - B - L - R|^2
+};
+
+// Potential sites grouped by type (potSites, potTypes).
+struct DevPotType {
+  int32_t element;
+  int32_t num_alphas;
+  int32_t first_site;
+  int32_t multiplicity;
+  int32_t cumul_alpha;
+  double nuc_charge;
+  double nuc_alpha;
+  double alphas[OLC_MAX_POT_ALPHAS];
+};
+
+// Everything a kernel needs about the system, passed by value.
+struct SysView {
+  const DevType* types;
+  const int32_t* site_type;
+  const double* site_pos;            // [3*n]
+  const int32_t* cum_vale;
+  const int32_t* cum_core;
+  const DevPair* pairs;
+  const DevTask* tasks;
+  const double* cells;               // [4*ncells] (x, y, z, |R|^2) sorted
+  int32_t ncells;
+  const DevPotType* pot_types;
+  int32_t num_pot_types;
+  const double* pot_site_pos;        // [3*npotsites]
+  const int32_t* pot_site_type;
+  int32_t num_pot_sites;
+  const double* elem_alpha;          // [nelem*OLC_MAX_ALPHAS]
+  const double* elem_nuc_alpha;      // [nelem]
+  const double* elem_pot_alpha;      // [nelem*OLC_MAX_POT_ALPHAS]
+  double inv_real[9];                // invRealVectors(i, xyz) row-major [abc][xyz]
+  double real_vec[9];                // [abc][xyz]
+  double log_thresh;                 // T = -ln(BASIS_FN thresh)
+  int32_t vale_dim, core_dim, nk;
+  const double* kxyz;                // [3*nk]
+  const double* phase;               // [nk*ncells] complex (re,im) : exp(i k.R)
+};
+
+// Items of the primitive stage: one per (task, alpha1, alpha2) grouped by
+// (l1, l2) class; within a class ordered by task.
+struct ItemLists {
+  int32_t count[kNumClasses];
+  int64_t sh_offset[kNumClasses];       // offset (doubles) of the class block in scratch
+  int32_t* task[kNumClasses];           // device arrays
+  int32_t* ab[kNumClasses];             // alpha1 | alpha2 << 8
+  int32_t* task_start[kNumClasses];     // [ntasks+1] start of each task's items
+  int64_t total_sh;                     // doubles of sh scratch
+};
+
+}  // namespace olc
+
+struct olc_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cublasHandle_t blas = nullptr;
+  cusolverDnHandle_t solver = nullptr;
+  // host copies
+  olc_dims_t dims{};
+  int nelem = 0;
+  std::vector<olc::DevType> htypes;
+  std::vector<olc::DevPotType> hpots;
+  std::vector<olc::DevPair> hpairs;
+  std::vector<olc::DevTask> htasks;
+  std::vector<double> hcells;
+  // device
+  olc::SysView view{};
+  std::vector<void*> allocations;
+  olc::ItemLists items{};
+  double* d_sh = nullptr;          // primitive sh scratch
+  double* d_block = nullptr;       // contracted (task, m1, m2) blocks
+  int64_t block_stride = 0;        // doubles per task block (MS*MS)
+  int max_states = 0;
+  // cached iteration-invariant data (olc_scf_prepare)
+  bool prepared = false;
+  int prep_precision = 0;
+  double* d_scv = nullptr;         // S core-vale  [nk][nv][nc] complex
+  double* d_h0 = nullptr;          // ortho(KE + NP) full upper [nk][nv][nv] complex
+  double* d_chol = nullptr;        // Cholesky factor of ortho'd S, [nk][nv][nv]
+  double* d_work_vv = nullptr;
+  double* d_work_cv = nullptr;
+  double* d_work_cc = nullptr;
+  double* d_work_x = nullptr;      // GEMM temporaries
+  double* d_work_y = nullptr;
+  double* d_work_w = nullptr;
+  void* d_solver_work = nullptr;
+  size_t solver_work_bytes = 0;
+  int* d_info = nullptr;
+  double* d_eval = nullptr;
+};
+
+namespace olc {
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_check(cudaError_t e, const char* what);
+
+// device allocation tracked by the context
+template <class T>
+int dalloc(olc_context* ctx, T** p, size_t count) {
+  void* q = nullptr;
+  if (count == 0) { *p = nullptr; return OLC_OK; }
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  if (e != cudaSuccess) return fail(OLC_ERR_ALLOC, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  ctx->allocations.push_back(q);
+  *p = static_cast<T*>(q);
+  return OLC_OK;
+}
+
+// host set-up (olc_setup.cpp)
+int build_system(olc_context* ctx, const olc_system_t* sys);
+
+// integral stages (olc_integrals.cu)
+int run_primitives(olc_context* ctx, int op, int term, const double* coeffs,
+                   int precision, bool accumulate);
+int run_contract_bloch(olc_context* ctx, double* vv, double* cv, double* cc);
+int primitive_batch_device(int kind, int n, const double* in, const int32_t* lmalpha,
+                           double* out);
+
+// dense stages (olc_linalg.cu)
+int ortho_pack(olc_context* ctx, bool is_overlap, double* vv, const double* cv,
+               const double* cc, const double* scv, double* packed, double* full_out);
+int assemble_packed(olc_context* ctx, const double* const* terms, const double* coeffs,
+                    int nterm, double* out);
+int solve_packed(olc_context* ctx, const double* packed_h, const double* packed_s,
+                 int num_states, double* eigenvalues, double* vectors, int32_t* info);
+int scf_prepare(olc_context* ctx, int precision);
+int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
+                  double* eigenvalues, int eig_on_device, double* vectors);
+
+}  // namespace olc

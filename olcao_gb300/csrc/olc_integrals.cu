@@ -1,0 +1,490 @@
+// Integral stages of the hot path on sm_103a.
+//
+// Stage 1 (primitive kernels, one thread per alpha-pair item, one launch per
+//   angular class so a warp runs one straight-line recurrence):  the reference's
+//   alpha loop body -- overlap2CIntg / kinetic2CIntg (integrals.F90:312-416)
+//   and the third-centre sums of nuclearPE / electronicPE (integrals.F90:
+//   2275-2598) -- producing the harmonic block sh(lm1, lm2) of each item in
+//   a scratch buffer.
+// Stage 2 (contraction, one warp per (pair, cell) task): the accumulation
+//   into pairXBasisFn2 and multWithBasisFn1 (integrals.F90:402-410,
+//   intgSaving.F90:56-89) as one sum over the task's items,
+//   block(m1,m2) = sum c1(a1,m1) c2(a2,m2) sh(lm(m1), lm(m2)).
+// Stage 3 (Bloch sum + scatter, one CTA per (pair, k range)):
+//   applyPhaseFactors, kPointLatticeOriginShift and saveCurrentPair
+//   (intgSaving.F90:95-505) -- out(m1,m2,k) = e^{ik.L} sum_R e^{ik.R} block_R
+//   written straight into valeVale / coreVale / coreCore.
+#include <cstdio>
+
+#include "olc_common.h"
+#include "olc_primitives.cuh"
+
+namespace olc {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double elem_alpha(const SysView& v, int e, int a) {
+  return v.elem_alpha[e * OLC_MAX_ALPHAS + a];
+}
+
+// alphaDist(a1, a2, e1, e2) of gaussRelations.f90:64-135 (same operation order)
+__device__ __forceinline__ double alpha_dist(const SysView& v, int a1, int a2, int e1, int e2) {
+  const double al = elem_alpha(v, e1, a1), ak = elem_alpha(v, e2, a2);
+  return v.log_thresh / ak / (al / (al + ak));
+}
+
+// Reduce v by the lattice vector obtained from rounding its fractional
+// coordinates (the first step of findLatticeVector, lattice.f90:777-793).
+__device__ __forceinline__ void round_reduce(const SysView& v, const double* in, double* out) {
+  double L[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double f = in[0] * v.inv_real[i * 3] + in[1] * v.inv_real[i * 3 + 1] +
+                     in[2] * v.inv_real[i * 3 + 2];
+    double r = floor(fabs(f) + 0.5);
+    if (f < 0.0) r = -r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) L[c] += v.real_vec[i * 3 + c] * r;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[c] = in[c] - L[c];
+}
+
+struct ItemGeom {
+  double A[3], B[3];
+  double a1, a2, sep;
+  int e1, e2, ia1, ia2;
+};
+
+__device__ __forceinline__ void load_item(const SysView& v, int task, int ab, ItemGeom& g) {
+  const DevTask tk = v.tasks[task];
+  const DevPair p = v.pairs[tk.pair];
+  const DevType& t1 = v.types[v.site_type[p.i]];
+  const DevType& t2 = v.types[v.site_type[p.j]];
+  g.ia1 = ab & 255;
+  g.ia2 = ab >> 8;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    g.A[c] = v.site_pos[3 * p.i + c];
+    g.B[c] = v.site_pos[3 * p.j + c] + p.L[c] + v.cells[4 * tk.cell + c];
+  }
+  g.a1 = t1.alphas[g.ia1];
+  g.a2 = t2.alphas[g.ia2];
+  g.e1 = t1.element;
+  g.e2 = t2.element;
+  g.sep = tk.sep;
+}
+
+// Visit every lattice image C' = C + T of a site with |P - C'|^2 <= tad.
+// The image set equals the reference's {cells of the nearest-origin loop},
+// integrals.F90:2374-2418 / 2533-2594.
+template <class F>
+__device__ __forceinline__ void for_images(const SysView& v, const double* P, const double* C,
+                                           double tad, F&& f) {
+  double d[3] = {P[0] - C[0], P[1] - C[1], P[2] - C[2]};
+  double r[3];
+  round_reduce(v, d, r);
+  const double rn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  const double lim = rn + sqrt(tad);
+  const double lim2 = lim * lim;
+  // base image of C: C + (d - r)
+  const double base[3] = {C[0] + (d[0] - r[0]), C[1] + (d[1] - r[1]), C[2] + (d[2] - r[2])};
+  for (int n = 0; n < v.ncells; ++n) {
+    const double4 cell = reinterpret_cast<const double4*>(v.cells)[n];
+    if (cell.w > lim2) break;
+    const double x = r[0] - cell.x, y = r[1] - cell.y, z = r[2] - cell.z;
+    const double d2 = x * x + y * y + z * z;
+    if (d2 > tad) continue;
+    const double Cp[3] = {base[0] + cell.x, base[1] + cell.y, base[2] + cell.z};
+    f(Cp, d2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stage 1: primitive kernels
+// ---------------------------------------------------------------------------
+struct PrimArgs {
+  const int32_t* task;
+  const int32_t* ab;
+  int n;
+  double* out;              // class block of the sh scratch
+  const double* coeffs;     // device [pot_dim] (EP) or nullptr
+  int accumulate;
+  int ep_type;              // EP: potential type of a single term, -1 = all types
+  int ep_alpha;             // EP: exponent index of a single term
+};
+
+template <int OP, int L1, int L2>
+__global__ void __launch_bounds__(128) prim_kernel(SysView v, PrimArgs a) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= a.n) return;
+  constexpr int N1 = ncart(L1), N2 = ncart(L2), NS = nharm(L1) * nharm(L2);
+  ItemGeom g;
+  load_item(v, a.task[idx], a.ab[idx], g);
+  double cart[N1 * N2];
+#pragma unroll
+  for (int q = 0; q < N1 * N2; ++q) cart[q] = 0.0;
+  double scale = 1.0;
+  if (OP == OLC_OP_OVERLAP) {
+    add_overlap<L1, L2>(g.a1, g.a2, g.A, g.B, 1.0, cart);
+  } else if (OP == OLC_OP_KINETIC) {
+    add_kinetic<L1, L2>(g.a1, g.a2, g.A, g.B, 1.0, cart);
+  } else {
+    // centre of the alpha-pair overlap (alphaCenter, gaussRelations.f90:122)
+    const double al = elem_alpha(v, g.e1, g.ia1), ak = elem_alpha(v, g.e2, g.ia2);
+    const double cen = al / (al + ak);
+    double P[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) P[c] = cen * (g.A[c] - g.B[c]) + g.B[c];
+    const double frac = 1.0 - g.sep / alpha_dist(v, g.ia1, g.ia2, g.e1, g.e2);
+    const double T = v.log_thresh;
+    if (OP == OLC_OP_NUCLEAR) {
+      for (int m = 0; m < v.num_pot_sites; ++m) {
+        const DevPotType& pt = v.pot_types[v.pot_site_type[m]];
+        if (pt.nuc_charge < 1.0e-8) continue;
+        const double an = v.elem_nuc_alpha[pt.element];
+        const double tad = frac * (T * (al + ak + an) / (al + ak) / an);
+        const double nz = -pt.nuc_charge, nalpha = pt.nuc_alpha;
+        for_images(v, P, &v.pot_site_pos[3 * m], tad, [&](const double* Cp, double) {
+          add_nuclear<L1, L2>(g.a1, g.a2, nalpha, g.A, g.B, Cp, nz, cart);
+        });
+      }
+    } else {  // electronic potential: single term or sum_j c_j V_j
+      double d2 = 0.0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) d2 += (g.A[c] - g.B[c]) * (g.A[c] - g.B[c]);
+      const double expAB = exp(-(g.a1 * g.a2 / (g.a1 + g.a2)) * d2);
+      const int t0 = a.ep_type < 0 ? 0 : a.ep_type;
+      const int t1 = a.ep_type < 0 ? v.num_pot_types : a.ep_type + 1;
+      for (int t = t0; t < t1; ++t) {
+        const DevPotType& pt = v.pot_types[t];
+        const double* pe = &v.elem_pot_alpha[pt.element * OLC_MAX_POT_ALPHAS];
+        const int j0 = a.ep_type < 0 ? 0 : a.ep_alpha;
+        const int j1 = a.ep_type < 0 ? pt.num_alphas : a.ep_alpha + 1;
+        // largest radius first: alphaPotDist decreases with the exponent
+        const double tad0 = frac * (T * (al + ak + pe[j0]) / (al + ak) / pe[j0]);
+        for (int m = 0; m < pt.multiplicity; ++m) {
+          const double* C = &v.pot_site_pos[3 * (pt.first_site + m)];
+          for_images(v, P, C, tad0, [&](const double* Cp, double dd) {
+            for (int j = j0; j < j1; ++j) {
+              const double tad = frac * (T * (al + ak + pe[j]) / (al + ak) / pe[j]);
+              if (dd > tad) break;
+              const double w = a.coeffs ? a.coeffs[pt.cumul_alpha + j] : 1.0;
+              add_elec3c<L1, L2, double>(g.a1, g.a2, pt.alphas[j], g.A, g.B, Cp, expAB, w, cart);
+            }
+          });
+        }
+      }
+    }
+  }
+  store_harmonic<L1, L2, double>(cart, a.out + (size_t)idx * NS, a.accumulate != 0, scale);
+}
+
+template <int OP>
+int launch_class(olc_context* ctx, int cls, const double* coeffs, int ep_type, int ep_alpha,
+                 bool accumulate) {
+  const ItemLists& it = ctx->items;
+  PrimArgs a;
+  a.task = it.task[cls];
+  a.ab = it.ab[cls];
+  a.n = it.count[cls];
+  a.out = ctx->d_sh + it.sh_offset[cls];
+  a.coeffs = coeffs;
+  a.accumulate = accumulate ? 1 : 0;
+  a.ep_type = ep_type;
+  a.ep_alpha = ep_alpha;
+  if (a.n == 0) return OLC_OK;
+  const dim3 block(128), grid((a.n + 127) / 128);
+  switch (cls) {
+#define OLC_CASE(c, l1, l2) \
+  case c: prim_kernel<OP, l1, l2><<<grid, block, 0, ctx->stream>>>(ctx->view, a); break;
+    OLC_CASE(0, 0, 0) OLC_CASE(1, 0, 1) OLC_CASE(2, 0, 2)
+    OLC_CASE(3, 1, 0) OLC_CASE(4, 1, 1) OLC_CASE(5, 1, 2)
+    OLC_CASE(6, 2, 0) OLC_CASE(7, 2, 1) OLC_CASE(8, 2, 2)
+#undef OLC_CASE
+  }
+  return cuda_check(cudaGetLastError(), "prim_kernel launch");
+}
+
+int run_primitives(olc_context* ctx, int op, int term, const double* coeffs, int precision,
+                   bool accumulate) {
+  int ep_type = -1, ep_alpha = 0;
+  if (op == OLC_OP_ELECPOT && !coeffs) {
+    ep_type = -2;
+    for (size_t t = 0; t < ctx->hpots.size(); ++t)
+      if (term >= ctx->hpots[t].cumul_alpha &&
+          term < ctx->hpots[t].cumul_alpha + ctx->hpots[t].num_alphas) {
+        ep_type = (int)t;
+        ep_alpha = term - ctx->hpots[t].cumul_alpha;
+      }
+    if (ep_type < 0) return fail(OLC_ERR_ARG, "potential term index out of range");
+  }
+  (void)precision;
+  for (int cls = 0; cls < kNumClasses; ++cls) {
+    int st = 0;
+    switch (op) {
+      case OLC_OP_OVERLAP: st = launch_class<OLC_OP_OVERLAP>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_KINETIC: st = launch_class<OLC_OP_KINETIC>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_NUCLEAR: st = launch_class<OLC_OP_NUCLEAR>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_ELECPOT: st = launch_class<OLC_OP_ELECPOT>(ctx, cls, coeffs, ep_type, ep_alpha, accumulate); break;
+      default: return fail(OLC_ERR_ARG, "unknown integral operator");
+    }
+    if (st) return st;
+  }
+  return OLC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage 2: contraction with the basis coefficients, one warp per task
+// ---------------------------------------------------------------------------
+struct ContractArgs {
+  const int32_t* ab[kNumClasses];
+  const int32_t* start[kNumClasses];
+  const double* sh[kNumClasses];
+  int ntasks;
+  int ms;                   // block stride (max states)
+  double* block;            // [task][m2*ms + m1]
+};
+
+__global__ void __launch_bounds__(256) contract_kernel(SysView v, ContractArgs a) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= a.ntasks) return;
+  const DevTask tk = v.tasks[warp];
+  const DevPair p = v.pairs[tk.pair];
+  const DevType& t1 = v.types[v.site_type[p.i]];
+  const DevType& t2 = v.types[v.site_type[p.j]];
+  const int M1 = t1.nstates, M2 = t2.nstates;
+  double* out = a.block + (size_t)warp * a.ms * a.ms;
+  for (int e = lane; e < M1 * M2; e += 32) {
+    const int m1 = e % M1, m2 = e / M1;
+    const int lm1 = t1.lm_index[m1] - 1, lm2 = t2.lm_index[m2] - 1;
+    double acc = 0.0;
+#pragma unroll
+    for (int cls = 0; cls < kNumClasses; ++cls) {
+      const int l1 = cls / (kMaxL + 1), l2 = cls % (kMaxL + 1);
+      const int ns1 = (l1 + 1) * (l1 + 1), ns2 = (l2 + 1) * (l2 + 1);
+      if (lm1 >= ns1 || lm2 >= ns2) continue;
+      const int b = a.start[cls][warp], en = a.start[cls][warp + 1];
+      const double* sh = a.sh[cls];
+      for (int q = b; q < en; ++q) {
+        const int ab = a.ab[cls][q];
+        const int a1 = ab & 255, a2 = ab >> 8;
+        acc += t1.basis[a1 * OLC_MAX_STATES + m1] * t2.basis[a2 * OLC_MAX_STATES + m2] *
+               sh[(size_t)q * ns1 * ns2 + lm2 * ns1 + lm1];
+      }
+    }
+    out[m2 * a.ms + m1] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stage 3: Bloch sum, lattice-origin phase and scatter
+// ---------------------------------------------------------------------------
+__global__ void phase_table_kernel(SysView v, double* phase) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= v.nk * v.ncells) return;
+  const int k = idx / v.ncells, n = idx % v.ncells;
+  const double kr = v.kxyz[3 * k] * v.cells[4 * n] + v.kxyz[3 * k + 1] * v.cells[4 * n + 1] +
+                    v.kxyz[3 * k + 2] * v.cells[4 * n + 2];
+  double s, c;
+  sincos(kr, &s, &c);
+  phase[2 * idx] = c;
+  phase[2 * idx + 1] = s;
+}
+
+struct BlochArgs {
+  const double* block;
+  int ms;
+  int kchunk;
+  double* vv;
+  double* cv;
+  double* cc;
+};
+
+__global__ void __launch_bounds__(256) bloch_scatter_kernel(SysView v, BlochArgs a) {
+  const DevPair p = v.pairs[blockIdx.x];
+  const DevType& t1 = v.types[v.site_type[p.i]];
+  const DevType& t2 = v.types[v.site_type[p.j]];
+  const int M1 = t1.nstates, M2 = t2.nstates;
+  const int k0 = blockIdx.y * a.kchunk;
+  const int k1 = min(v.nk, k0 + a.kchunk);
+  const int per_k = M1 * M2;
+  const int total = per_k * (k1 - k0);
+  const size_t nv = v.vale_dim, nc = v.core_dim;
+  const bool same = (p.i == p.j);
+  const int vi1 = v.cum_vale[p.i], vi2 = v.cum_vale[p.j];
+  const int ci1 = v.cum_core[p.i], ci2 = v.cum_core[p.j];
+  const int vn1 = t1.nvale, vn2 = t2.nvale;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int k = k0 + e / per_k;
+    const int r = e % per_k;
+    const int m1 = r % M1, m2 = r / M1;
+    double re = 0.0, im = 0.0;
+    const double* ph = v.phase + 2 * (size_t)k * v.ncells;
+    for (int t = p.task_begin; t < p.task_end; ++t) {
+      const int cell = v.tasks[t].cell;
+      const double b = a.block[(size_t)t * a.ms * a.ms + m2 * a.ms + m1];
+      re += ph[2 * cell] * b;
+      im += ph[2 * cell + 1] * b;
+    }
+    const double kl = v.kxyz[3 * k] * p.L[0] + v.kxyz[3 * k + 1] * p.L[1] + v.kxyz[3 * k + 2] * p.L[2];
+    if (kl != 0.0) {
+      double s, c;
+      sincos(kl, &s, &c);
+      const double nr = c * re - s * im, ni = s * re + c * im;
+      re = nr;
+      im = ni;
+    }
+    // saveCurrentPair (intgSaving.F90:201-505)
+    if (m1 < vn1 && m2 < vn2) {
+      const size_t row = vi1 + m1, col = vi2 + m2;
+      double* d = a.vv + 2 * ((size_t)k * nv * nv + col * nv + row);
+      if (same && m1 > m2) { d[0] = 0.0; d[1] = 0.0; }
+      else { d[0] = re; d[1] = im; }
+    } else if (m1 >= vn1 && m2 < vn2) {
+      if (!same) {
+        double* d = a.cv + 2 * ((size_t)k * nc * nv + (size_t)(vi2 + m2) * nc + ci1 + (m1 - vn1));
+        d[0] = re;
+        d[1] = im;
+      }
+    } else if (m1 < vn1 && m2 >= vn2) {
+      double* d = a.cv + 2 * ((size_t)k * nc * nv + (size_t)(vi1 + m1) * nc + ci2 + (m2 - vn2));
+      d[0] = re;
+      d[1] = -im;
+    } else {
+      const int c1 = m1 - vn1, c2 = m2 - vn2;
+      double* d = a.cc + 2 * ((size_t)k * nc * nc + (size_t)(ci2 + c2) * nc + ci1 + c1);
+      d[0] = re;
+      d[1] = im;
+      if (!same) {
+        double* e2 = a.cc + 2 * ((size_t)k * nc * nc + (size_t)(ci1 + c1) * nc + ci2 + c2);
+        e2[0] = re;
+        e2[1] = -im;
+      }
+    }
+  }
+}
+
+int run_contract_bloch(olc_context* ctx, double* vv, double* cv, double* cc) {
+  const SysView& v = ctx->view;
+  const int ntasks = ctx->dims.num_pair_tasks;
+  const size_t nv = v.vale_dim, nc = v.core_dim, nk = v.nk;
+  int st;
+  if ((st = cuda_check(cudaMemsetAsync(vv, 0, 16 * nv * nv * nk, ctx->stream), "memset vv"))) return st;
+  if (nc) {
+    if (!cv || !cc) return fail(OLC_ERR_ARG, "core outputs required when core_dim > 0");
+    if ((st = cuda_check(cudaMemsetAsync(cv, 0, 16 * nc * nv * nk, ctx->stream), "memset cv"))) return st;
+    if ((st = cuda_check(cudaMemsetAsync(cc, 0, 16 * nc * nc * nk, ctx->stream), "memset cc"))) return st;
+  }
+  if (ntasks == 0) return OLC_OK;
+  ContractArgs ca;
+  for (int c = 0; c < kNumClasses; ++c) {
+    ca.ab[c] = ctx->items.ab[c];
+    ca.start[c] = ctx->items.task_start[c];
+    ca.sh[c] = ctx->d_sh + ctx->items.sh_offset[c];
+  }
+  ca.ntasks = ntasks;
+  ca.ms = ctx->max_states;
+  ca.block = ctx->d_block;
+  contract_kernel<<<(ntasks + 7) / 8, 256, 0, ctx->stream>>>(v, ca);
+  if ((st = cuda_check(cudaGetLastError(), "contract_kernel"))) return st;
+  BlochArgs ba;
+  ba.block = ctx->d_block;
+  ba.ms = ctx->max_states;
+  const int per_k = ctx->max_states * ctx->max_states;
+  ba.kchunk = std::max(1, std::min((int)nk, 2048 / std::max(1, per_k)));
+  ba.vv = vv;
+  ba.cv = cv;
+  ba.cc = cc;
+  dim3 grid((unsigned)ctx->hpairs.size(), (unsigned)((nk + ba.kchunk - 1) / ba.kchunk));
+  bloch_scatter_kernel<<<grid, 256, 0, ctx->stream>>>(v, ba);
+  return cuda_check(cudaGetLastError(), "bloch_scatter_kernel");
+}
+
+int build_phase_table(olc_context* ctx) {
+  const SysView& v = ctx->view;
+  const int n = v.nk * v.ncells;
+  phase_table_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(v, const_cast<double*>(v.phase));
+  return cuda_check(cudaGetLastError(), "phase_table_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// primitive batch (testing entry): explicit inputs, one thread per primitive
+// ---------------------------------------------------------------------------
+template <int L1, int L2>
+__device__ void prim_one(int kind, const double* in, double* out) {
+  constexpr int N1 = ncart(L1), N2 = ncart(L2), NS1 = nharm(L1), NS2 = nharm(L2);
+  double cart[N1 * N2];
+#pragma unroll
+  for (int q = 0; q < N1 * N2; ++q) cart[q] = 0.0;
+  const double *A = in + 3, *B = in + 6, *C = in + 9;
+  if (kind == 1) add_overlap<L1, L2>(in[0], in[1], A, B, 1.0, cart);
+  else if (kind == 2) add_kinetic<L1, L2>(in[0], in[1], A, B, 1.0, cart);
+  else if (kind == 3) add_nuclear<L1, L2>(in[0], in[1], in[2], A, B, C, 1.0, cart);
+  else {
+    double d2 = 0.0;
+    for (int c = 0; c < 3; ++c) d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    const double expAB = exp(-(in[0] * in[1] / (in[0] + in[1])) * d2);
+    add_elec3c<L1, L2, double>(in[0], in[1], in[2], A, B, C, expAB, 1.0, cart);
+  }
+  double sh[NS1 * NS2];
+  store_harmonic<L1, L2, double>(cart, sh, false, 1.0);
+  for (int q = 0; q < NS2; ++q)
+    for (int p2 = 0; p2 < NS1; ++p2) out[q * 16 + p2] = sh[q * NS1 + p2];
+}
+
+__global__ void prim_batch_kernel(int kind, int n, const double* in, const int32_t* lm,
+                                  double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  auto lof = [](int lma) { return lma == 1 ? 0 : lma == 4 ? 1 : 2; };
+  const int c = lof(lm[2 * i]) * 3 + lof(lm[2 * i + 1]);
+  const double* x = in + 12 * i;
+  double* o = out + 256 * i;
+  switch (c) {
+    case 0: prim_one<0, 0>(kind, x, o); break;
+    case 1: prim_one<0, 1>(kind, x, o); break;
+    case 2: prim_one<0, 2>(kind, x, o); break;
+    case 3: prim_one<1, 0>(kind, x, o); break;
+    case 4: prim_one<1, 1>(kind, x, o); break;
+    case 5: prim_one<1, 2>(kind, x, o); break;
+    case 6: prim_one<2, 0>(kind, x, o); break;
+    case 7: prim_one<2, 1>(kind, x, o); break;
+    case 8: prim_one<2, 2>(kind, x, o); break;
+  }
+}
+
+int primitive_batch_device(int kind, int n, const double* in, const int32_t* lmalpha,
+                           double* out) {
+  if (kind < 1 || kind > 4 || n < 0) return fail(OLC_ERR_ARG, "olc_primitive_batch: bad kind");
+  for (int i = 0; i < n; ++i) {
+    for (int s = 0; s < 2; ++s) {
+      int l = lmalpha[2 * i + s];
+      if (l != 1 && l != 4 && l != 9)
+        return fail(l == 16 ? OLC_ERR_UNSUPPORTED : OLC_ERR_ARG, "lmalpha must be 1, 4 or 9");
+    }
+  }
+  if (n == 0) return OLC_OK;
+  double *din = nullptr, *dout = nullptr;
+  int32_t* dlm = nullptr;
+  int st = OLC_OK;
+  if ((st = cuda_check(cudaMalloc(&din, sizeof(double) * 12 * n), "malloc"))) return st;
+  if ((st = cuda_check(cudaMalloc(&dout, sizeof(double) * 256 * n), "malloc"))) { cudaFree(din); return st; }
+  if ((st = cuda_check(cudaMalloc(&dlm, sizeof(int32_t) * 2 * n), "malloc"))) { cudaFree(din); cudaFree(dout); return st; }
+  st = cuda_check(cudaMemcpy(din, in, sizeof(double) * 12 * n, cudaMemcpyHostToDevice), "copy");
+  if (!st) st = cuda_check(cudaMemcpy(dlm, lmalpha, sizeof(int32_t) * 2 * n, cudaMemcpyHostToDevice), "copy");
+  if (!st) st = cuda_check(cudaMemset(dout, 0, sizeof(double) * 256 * n), "memset");
+  if (!st) {
+    prim_batch_kernel<<<(n + 63) / 64, 64>>>(kind, n, din, dlm, dout);
+    st = cuda_check(cudaGetLastError(), "prim_batch_kernel");
+  }
+  if (!st) st = cuda_check(cudaMemcpy(out, dout, sizeof(double) * 256 * n, cudaMemcpyDeviceToHost), "copy back");
+  cudaFree(din);
+  cudaFree(dout);
+  cudaFree(dlm);
+  return st;
+}
+
+}  // namespace olc

@@ -1,0 +1,410 @@
+// Dense stages of the hot path: valence-core orthogonalisation and packing,
+// Hamiltonian assembly, and the per-k generalised Hermitian eigen-solve.
+//
+//   ortho + pack     intgOrtho.F90:23-187 with integrals.F90:2601-2853:
+//                    O' = O_vv - (S_cv^H O_cv + O_cv^H S_cv) + S_cv^H O_cc S_cv
+//                    (S' = S_vv - 2 S_cv^H S_cv + S_cv^H S_cc S_cv), upper
+//                    triangle, diagonal made real as zherk/zher2k do, packed
+//                    column by column with |x| < 1e-10 flushed when core_dim > 0.
+//   assembly         secularEqn.F90:128-166, matrixSubs.F90:248-355.
+//   solve            solveZHEGV, interfaces.F90:73-120 (itype 1, 'V', 'U').
+// The GEMMs are FP64 complex library GEMMs (cuBLAS); the epilogue that
+// combines, flushes and packs is a hand-written kernel; the small-n solves
+// use a batched in-shared-memory kernel (olc_eigen_small.cu).
+#include <algorithm>
+#include <cstdio>
+
+#include "olc_common.h"
+
+namespace olc {
+
+int solve_small_batched(olc_context* ctx, const double* h_full, const double* s_full, int n,
+                        int num_states, double* eigenvalues, double* vectors, int32_t* info_host,
+                        bool s_is_factored);
+int small_solver_max_n();
+
+namespace {
+
+// combine, flush and pack; optionally also emit the full upper matrix (+ add)
+struct PackArgs {
+  const double* vv;      // [nk][nv][nv]
+  const double* X;       // S_cv^H O_cv          (nullptr when nc == 0)
+  const double* Y;       // S_cv^H O_cc S_cv
+  const double* add;     // optional full upper matrix added after the flush
+  double* packed;        // [nk][plen][2] or nullptr
+  double* full;          // [nk][nv][nv] upper, or nullptr
+  int nv;
+  int nk;
+  int nc;
+  int is_overlap;
+};
+
+__global__ void ortho_pack_kernel(PackArgs a) {
+  const size_t plen = (size_t)a.nv * (a.nv + 1) / 2;
+  const size_t total = plen * a.nk;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / plen);
+    const size_t r = idx % plen;
+    // column i, row j <= i with r = i(i+1)/2 + j
+    int i = (int)((sqrt(8.0 * (double)r + 1.0) - 1.0) * 0.5);
+    while ((size_t)i * (i + 1) / 2 > r) --i;
+    while ((size_t)(i + 1) * (i + 2) / 2 <= r) ++i;
+    const int j = (int)(r - (size_t)i * (i + 1) / 2);
+    const size_t nn = (size_t)a.nv * a.nv;
+    const size_t off = (size_t)k * nn + (size_t)i * a.nv + j;   // (row j, col i)
+    double re = a.vv[2 * off], im = a.vv[2 * off + 1];
+    if (a.nc) {
+      const double xr = a.X[2 * off], xi = a.X[2 * off + 1];
+      if (a.is_overlap) {   // zherk('U','C',-2)
+        re -= 2.0 * xr;
+        im -= 2.0 * xi;
+      } else {              // zher2k('U','C',-1): X + X^H
+        const size_t offT = (size_t)k * nn + (size_t)j * a.nv + i;
+        re -= xr + a.X[2 * offT];
+        im -= xi - a.X[2 * offT + 1];
+      }
+      if (i == j) im = 0.0;
+      re += a.Y[2 * off];
+      im += a.Y[2 * off + 1];
+      if (fabs(re) < 1.0e-10) re = 0.0;
+      if (fabs(im) < 1.0e-10) im = 0.0;
+    }
+    if (a.packed) {
+      a.packed[2 * idx] = re;
+      a.packed[2 * idx + 1] = im;
+    }
+    if (a.full) {
+      if (a.add) {
+        re += a.add[2 * off];
+        im += a.add[2 * off + 1];
+      }
+      a.full[2 * off] = re;
+      a.full[2 * off + 1] = im;
+    }
+  }
+}
+
+// packed [nk][plen][2] -> full Hermitian [nk][n][n] (both triangles)
+__global__ void unpack_kernel(const double* packed, double* full, int n, int nk) {
+  const size_t nn = (size_t)n * n;
+  const size_t total = nn * nk;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / nn);
+    const size_t r = idx % nn;
+    const int col = (int)(r / n), row = (int)(r % n);
+    const int i = max(row, col), j = min(row, col);
+    const size_t p = (size_t)k * ((size_t)n * (n + 1) / 2) + (size_t)i * (i + 1) / 2 + j;
+    double re = packed[2 * p], im = packed[2 * p + 1];
+    if (row > col) im = -im;
+    if (row == col) im = 0.0;
+    full[2 * idx] = re;
+    full[2 * idx + 1] = im;
+  }
+}
+
+// upper-only full matrix -> Hermitian (fill the strict lower triangle)
+__global__ void hermitize_kernel(double* full, int n, int nk) {
+  const size_t nn = (size_t)n * n;
+  const size_t total = nn * nk;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / nn);
+    const size_t r = idx % nn;
+    const int col = (int)(r / n), row = (int)(r % n);
+    if (row > col) {
+      const size_t src = (size_t)k * nn + (size_t)row * n + col;
+      full[2 * idx] = full[2 * src];
+      full[2 * idx + 1] = -full[2 * src + 1];
+    } else if (row == col) {
+      full[2 * idx + 1] = 0.0;
+    }
+  }
+}
+
+// H packed = NP + KE + sum c_j V_j (zero multiplier adds unscaled)
+__global__ void assemble_kernel(const double* const* terms, const double* coeffs, int nterm,
+                                size_t len, double* out) {
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < len;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    double acc = terms[0][idx];
+    for (int t = 1; t < nterm; ++t) {
+      const double c = coeffs[t];
+      const double x = terms[t][idx];
+      acc = (c == 0.0) ? acc + x : acc + x * c;
+    }
+    out[idx] = acc;
+  }
+}
+
+__global__ void gather_eigs_kernel(const double* w, int n, int nstates, int k, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nstates) out[(size_t)k * nstates + i] = w[i];
+}
+
+int grid_for(size_t n) {
+  size_t g = (n + 255) / 256;
+  return (int)std::min<size_t>(g, 152 * 32);
+}
+
+}  // namespace
+
+// Orthogonalise one operator for all k.  vv/cv/cc are the operator's blocks,
+// scv is S_cv.  Writes packed and/or full (upper, with `add` added).
+int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const double* cv,
+                  const double* cc, const double* scv, double* packed, double* full,
+                  const double* add) {
+  const int nv = ctx->dims.vale_dim, nc = ctx->dims.core_dim, nk = ctx->dims.num_kpoints;
+  int st;
+  if (nc) {
+    const size_t nn = (size_t)nv * nv;
+    if (!ctx->d_work_x) {
+      if ((st = dalloc(ctx, &ctx->d_work_x, 2 * nn * nk))) return st;
+      if ((st = dalloc(ctx, &ctx->d_work_y, 2 * nn * nk))) return st;
+      if ((st = dalloc(ctx, &ctx->d_work_w, 2 * (size_t)nv * nc * nk))) return st;
+    }
+    const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0);
+    const cuDoubleComplex zero = make_cuDoubleComplex(0.0, 0.0);
+    const auto* S = reinterpret_cast<const cuDoubleComplex*>(scv);
+    const auto* O = reinterpret_cast<const cuDoubleComplex*>(cv);
+    const auto* CC = reinterpret_cast<const cuDoubleComplex*>(cc);
+    auto* X = reinterpret_cast<cuDoubleComplex*>(ctx->d_work_x);
+    auto* Y = reinterpret_cast<cuDoubleComplex*>(ctx->d_work_y);
+    auto* W = reinterpret_cast<cuDoubleComplex*>(ctx->d_work_w);
+    const long long sCV = (long long)nc * nv, sCC = (long long)nc * nc, sVV = (long long)nn,
+                    sW = (long long)nv * nc;
+    cublasStatus_t bs;
+    // X = S_cv^H O_cv
+    bs = cublasZgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nv, nv, nc, &one, S, nc,
+                                   sCV, is_overlap ? S : O, nc, sCV, &zero, X, nv, sVV, nk);
+    if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cublasZgemm (X) failed");
+    // W = S_cv^H O_cc
+    bs = cublasZgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nv, nc, nc, &one, S, nc,
+                                   sCV, CC, nc, sCC, &zero, W, nv, sW, nk);
+    if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cublasZgemm (W) failed");
+    // Y = W S_cv
+    bs = cublasZgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, nv, nv, nc, &one, W, nv,
+                                   sW, S, nc, sCV, &zero, Y, nv, sVV, nk);
+    if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cublasZgemm (Y) failed");
+  }
+  PackArgs a;
+  a.vv = vv;
+  a.X = ctx->d_work_x;
+  a.Y = ctx->d_work_y;
+  a.add = add;
+  a.packed = packed;
+  a.full = full;
+  a.nv = nv;
+  a.nk = nk;
+  a.nc = nc;
+  a.is_overlap = is_overlap ? 1 : 0;
+  const size_t total = (size_t)nv * (nv + 1) / 2 * nk;
+  ortho_pack_kernel<<<grid_for(total), 256, 0, ctx->stream>>>(a);
+  return cuda_check(cudaGetLastError(), "ortho_pack_kernel");
+}
+
+int ortho_pack(olc_context* ctx, bool is_overlap, double* vv, const double* cv, const double* cc,
+               const double* scv, double* packed, double* full_out) {
+  return ortho_pack_ex(ctx, is_overlap, vv, cv, cc, is_overlap ? cv : scv, packed, full_out,
+                       nullptr);
+}
+
+int assemble_packed(olc_context* ctx, const double* const* terms, const double* coeffs, int nterm,
+                    double* out) {
+  if (nterm < 1) return fail(OLC_ERR_ARG, "assemble: need at least one term");
+  const size_t len = 2 * (size_t)ctx->dims.packed_len * ctx->dims.num_kpoints;
+  const double** dterms = nullptr;
+  double* dco = nullptr;
+  int st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&dterms, sizeof(double*) * nterm, ctx->stream), "malloc"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * nterm, ctx->stream), "malloc"))) return st;
+  cudaMemcpyAsync(dterms, terms, sizeof(double*) * nterm, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dco, coeffs, sizeof(double) * nterm, cudaMemcpyHostToDevice, ctx->stream);
+  assemble_kernel<<<grid_for(len), 256, 0, ctx->stream>>>(dterms, dco, nterm, len, out);
+  st = cuda_check(cudaGetLastError(), "assemble_kernel");
+  cudaFreeAsync(dterms, ctx->stream);
+  cudaFreeAsync(dco, ctx->stream);
+  if (!st) st = cuda_check(cudaStreamSynchronize(ctx->stream), "assemble sync");
+  return st;
+}
+
+// Generalised eigen-problem per k on full Hermitian matrices h, s (both
+// overwritten).  Library path: cuSOLVER zhegvd (same algorithm as LAPACK
+// zhegv: Cholesky, reduction, tridiagonal solve, back-transform).
+int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
+                       double* eigenvalues, int eig_on_device, double* vectors, int32_t* info) {
+  const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
+  const size_t nn = (size_t)n * n;
+  int st;
+  if (!ctx->d_eval) {
+    if ((st = dalloc(ctx, &ctx->d_eval, (size_t)n))) return st;
+    if ((st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
+  }
+  int lwork = 0;
+  cusolverStatus_t ss = cusolverDnZhegvd_bufferSize(
+      ctx->solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+      reinterpret_cast<cuDoubleComplex*>(h), n, reinterpret_cast<cuDoubleComplex*>(s), n,
+      ctx->d_eval, &lwork);
+  if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "zhegvd_bufferSize failed");
+  const size_t need = sizeof(cuDoubleComplex) * (size_t)lwork;
+  if (need > ctx->solver_work_bytes) {
+    if (ctx->d_solver_work) cudaFree(ctx->d_solver_work);
+    ctx->d_solver_work = nullptr;
+    if ((st = cuda_check(cudaMalloc(&ctx->d_solver_work, need), "solver work"))) return st;
+    ctx->solver_work_bytes = need;
+  }
+  double* eig_dev = eigenvalues;
+  double* tmp_eigs = nullptr;
+  if (!eig_on_device) {
+    if ((st = cuda_check(cudaMallocAsync((void**)&tmp_eigs, sizeof(double) * (size_t)num_states * nk,
+                                         ctx->stream), "malloc eigs"))) return st;
+    eig_dev = tmp_eigs;
+  }
+  for (int k = 0; k < nk; ++k) {
+    auto* H = reinterpret_cast<cuDoubleComplex*>(h) + (size_t)k * nn;
+    auto* S = reinterpret_cast<cuDoubleComplex*>(s) + (size_t)k * nn;
+    ss = cusolverDnZhegvd(ctx->solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                          CUBLAS_FILL_MODE_UPPER, n, H, n, S, n, ctx->d_eval,
+                          reinterpret_cast<cuDoubleComplex*>(ctx->d_solver_work), lwork,
+                          ctx->d_info + k);
+    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnZhegvd failed");
+    gather_eigs_kernel<<<(num_states + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_eval, n,
+                                                                          num_states, k, eig_dev);
+    if (vectors)
+      cudaMemcpyAsync(vectors + 2 * (size_t)k * n * num_states, H,
+                      sizeof(cuDoubleComplex) * (size_t)n * num_states, cudaMemcpyDeviceToDevice,
+                      ctx->stream);
+  }
+  if (!eig_on_device) {
+    cudaMemcpyAsync(eigenvalues, tmp_eigs, sizeof(double) * (size_t)num_states * nk,
+                    cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(tmp_eigs, ctx->stream);
+  }
+  std::vector<int> hinfo(nk);
+  cudaMemcpyAsync(hinfo.data(), ctx->d_info, sizeof(int) * nk, cudaMemcpyDeviceToHost, ctx->stream);
+  if ((st = cuda_check(cudaStreamSynchronize(ctx->stream), "solve sync"))) return st;
+  int worst = 0;
+  for (int k = 0; k < nk; ++k) {
+    if (info) info[k] = hinfo[k];
+    if (hinfo[k] != 0 && worst == 0) worst = hinfo[k];
+  }
+  if (worst > n) return fail(OLC_ERR_NOT_PD, "ZHEGV: overlap matrix not positive definite");
+  if (worst != 0) return fail(OLC_ERR_EIGEN, "ZHEGV: eigen-solver did not converge");
+  return OLC_OK;
+}
+
+int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* eigenvalues,
+               int eig_on_device, double* vectors, int32_t* info) {
+  const int n = ctx->dims.vale_dim;
+  if (n <= small_solver_max_n()) {
+    int st;
+    double* eig_dev = eigenvalues;
+    double* tmp = nullptr;
+    const int nk = ctx->dims.num_kpoints;
+    if (!eig_on_device) {
+      if ((st = cuda_check(cudaMallocAsync((void**)&tmp, sizeof(double) * (size_t)num_states * nk,
+                                           ctx->stream), "malloc eigs"))) return st;
+      eig_dev = tmp;
+    }
+    st = solve_small_batched(ctx, h, s, n, num_states, eig_dev, vectors, info, false);
+    if (!eig_on_device) {
+      cudaMemcpyAsync(eigenvalues, tmp, sizeof(double) * (size_t)num_states * nk,
+                      cudaMemcpyDeviceToHost, ctx->stream);
+      cudaFreeAsync(tmp, ctx->stream);
+      int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "eig copy");
+      if (!st) st = s2;
+    }
+    return st;
+  }
+  return solve_full_library(ctx, h, s, num_states, eigenvalues, eig_on_device, vectors, info);
+}
+
+int solve_packed(olc_context* ctx, const double* packed_h, const double* packed_s, int num_states,
+                 double* eigenvalues, double* vectors, int32_t* info) {
+  const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
+  if (num_states < 1 || num_states > n) return fail(OLC_ERR_ARG, "num_states out of range");
+  const size_t nn = (size_t)n * n;
+  double *h = nullptr, *s = nullptr;
+  int st;
+  if ((st = cuda_check(cudaMalloc(&h, 16 * nn * nk), "malloc h"))) return st;
+  if ((st = cuda_check(cudaMalloc(&s, 16 * nn * nk), "malloc s"))) { cudaFree(h); return st; }
+  unpack_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(packed_h, h, n, nk);
+  unpack_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(packed_s, s, n, nk);
+  st = cuda_check(cudaGetLastError(), "unpack_kernel");
+  if (!st) st = solve_full(ctx, h, s, num_states, eigenvalues, 1, vectors, info);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(h);
+  cudaFree(s);
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// SCF pass
+// ---------------------------------------------------------------------------
+int scf_prepare(olc_context* ctx, int precision) {
+  const int nv = ctx->dims.vale_dim, nc = ctx->dims.core_dim, nk = ctx->dims.num_kpoints;
+  const size_t nn = (size_t)nv * nv;
+  int st;
+  if (!ctx->d_work_vv) {
+    if ((st = dalloc(ctx, &ctx->d_work_vv, 2 * nn * nk))) return st;
+    if (nc) {
+      if ((st = dalloc(ctx, &ctx->d_work_cv, 2 * (size_t)nc * nv * nk))) return st;
+      if ((st = dalloc(ctx, &ctx->d_work_cc, 2 * (size_t)nc * nc * nk))) return st;
+      if ((st = dalloc(ctx, &ctx->d_scv, 2 * (size_t)nc * nv * nk))) return st;
+    }
+    if ((st = dalloc(ctx, &ctx->d_h0, 2 * nn * nk))) return st;
+    if ((st = dalloc(ctx, &ctx->d_chol, 2 * nn * nk))) return st;   // orthogonalised S
+  }
+  // S: overlap integrals, keep S_cv, orthogonalise
+  if ((st = run_primitives(ctx, OLC_OP_OVERLAP, 0, nullptr, OLC_PREC_FP64, false))) return st;
+  if ((st = run_contract_bloch(ctx, ctx->d_work_vv, nc ? ctx->d_scv : nullptr, ctx->d_work_cc))) return st;
+  if ((st = ortho_pack_ex(ctx, true, ctx->d_work_vv, ctx->d_scv, ctx->d_work_cc, ctx->d_scv,
+                          nullptr, ctx->d_chol, nullptr))) return st;
+  // H0 = KE + NP in one pass
+  if ((st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, OLC_PREC_FP64, false))) return st;
+  if ((st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, OLC_PREC_FP64, true))) return st;
+  if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
+  if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
+                          nullptr, ctx->d_h0, nullptr))) return st;
+  ctx->prepared = true;
+  ctx->prep_precision = precision;
+  return cuda_check(cudaStreamSynchronize(ctx->stream), "prepare sync");
+}
+
+int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
+                  double* eigenvalues, int eig_on_device, double* vectors) {
+  if (!ctx->prepared) return fail(OLC_ERR_ARG, "olc_scf_iteration before olc_scf_prepare");
+  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints, pd = ctx->dims.pot_dim;
+  if (num_states < 1 || num_states > nv) return fail(OLC_ERR_ARG, "num_states out of range");
+  const size_t nn = (size_t)nv * nv;
+  int st;
+  // the reference adds a term with multiplier 0 unscaled (matrixSubs.F90:278-282)
+  std::vector<double> c(coeffs, coeffs + pd);
+  for (auto& x : c)
+    if (x == 0.0) x = 1.0;
+  double* dco = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * std::max(1, pd), ctx->stream), "malloc coeffs"))) return st;
+  cudaMemcpyAsync(dco, c.data(), sizeof(double) * pd, cudaMemcpyHostToDevice, ctx->stream);
+  st = run_primitives(ctx, OLC_OP_ELECPOT, 0, dco, precision, false);
+  cudaFreeAsync(dco, ctx->stream);
+  if (st) return st;
+  if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
+  // H' = ortho(V) + H0 written into the work matrix (upper), S' copied
+  double *h = nullptr, *s = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
+  if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
+                          nullptr, h, ctx->d_h0))) return st;
+  cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
+  hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(h, nv, nk);
+  hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(s, nv, nk);
+  if ((st = cuda_check(cudaGetLastError(), "hermitize"))) return st;
+  st = solve_full(ctx, h, s, num_states, eigenvalues, eig_on_device, vectors, nullptr);
+  cudaFreeAsync(h, ctx->stream);
+  cudaFreeAsync(s, ctx->stream);
+  int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "iteration sync");
+  return st ? st : s2;
+}
+
+}  // namespace olc

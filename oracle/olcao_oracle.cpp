@@ -1,0 +1,915 @@
+// Tier-2 oracle: CPU FP64 restatement of OLCAO's per-SCF-iteration hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is compiled into oracle/_build/
+// liboracle.so and is called by tests/, __graft_entry__.smoke() and the
+// cpu_baseline leg of bench.py as the checker.  The product never links it.
+//
+// It restates, loop for loop and with the same screening order:
+//   lattice set-up            src/olcao/lattice.f90:229-286, 300-432, 456-747
+//   nearest lattice vector    src/olcao/lattice.f90:750-838 (see note below)
+//   k-points and phases       src/olcao/kpoints.f90:251-310
+//   basis                     src/olcao/basis.f90:55-243
+//   screening tables          src/olcao/gaussRelations.f90:64-278
+//   integral drivers          src/olcao/integrals.F90:81-486 (OL), 490-900 (KE),
+//                             1324-1715 (NP), 1719-2122 (EP), 2275-2439
+//                             (nuclearPE), 2442-2598 (electronicPE)
+//   pair scatter / phases     src/olcao/intgSaving.F90:56-550
+//   orthogonalisation, pack   src/olcao/intgOrtho.F90:23-187,
+//                             src/olcao/integrals.F90:2601-2853
+// Its Gaussian primitives are an independent Obara-Saika implementation
+// (Obara & Saika, J. Chem. Phys. 84, 3963 (1986)) checked against the
+// reference's own generated code (gaussIntegrals.f90) through the golden
+// vectors in tests/golden/.
+//
+// Notes on deliberate restatement choices (results identical up to rounding):
+// * findLatticeVector: the reference rounds each fractional coordinate and then
+//   consults Wigner-Seitz octant tables to land on the nearest lattice point;
+//   here the rounded point is refined by an explicit search over the nearest
+//   cells.  Either way the pair/third-centre image sets are
+//   {T : |A - B - T|^2 <= limit}, independent of the origin choice.
+// * The electronic-potential cell bit mask (integrals.F90:2074-2076,
+//   2230-2272) only skips cells that contribute nothing (threeAlphaDist is
+//   monotone in the potential exponent), so cells are tested directly.
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../include/olcao_gpu.h"
+
+namespace {
+
+using cplx = std::complex<double>;
+const double kPi = 3.141592653589793;
+
+// ---------------------------------------------------------------------------
+// Real-harmonic index tables (sh ordering of gaussIntegrals.f90:33-35).
+// Each sh component is a sum of coefficient * x^i y^j z^k monomials.
+// ---------------------------------------------------------------------------
+struct Mono { int e[3]; double c; };
+struct Harm { int n; Mono m[3]; };
+
+const Harm kHarm[16] = {
+    {1, {{{0, 0, 0}, 1.0}}},                                         // s
+    {1, {{{1, 0, 0}, 1.0}}},                                         // x
+    {1, {{{0, 1, 0}, 1.0}}},                                         // y
+    {1, {{{0, 0, 1}, 1.0}}},                                         // z
+    {1, {{{1, 1, 0}, 1.0}}},                                         // xy
+    {1, {{{1, 0, 1}, 1.0}}},                                         // xz
+    {1, {{{0, 1, 1}, 1.0}}},                                         // yz
+    {2, {{{2, 0, 0}, 1.0}, {{0, 2, 0}, -1.0}}},                      // xx-yy
+    {3, {{{0, 0, 2}, 2.0}, {{2, 0, 0}, -1.0}, {{0, 2, 0}, -1.0}}},   // 2zz-xx-yy
+    {1, {{{1, 1, 1}, 1.0}}},                                         // xyz
+    {2, {{{2, 0, 1}, 1.0}, {{0, 2, 1}, -1.0}}},                      // xxz-yyz
+    {2, {{{3, 0, 0}, 1.0}, {{1, 2, 0}, -3.0}}},                      // xxx-3yyx
+    {2, {{{2, 1, 0}, 3.0}, {{0, 3, 0}, -1.0}}},                      // 3xxy-yyy
+    {3, {{{0, 0, 3}, 2.0}, {{2, 0, 1}, -3.0}, {{0, 2, 1}, -3.0}}},   // 2zzz-3xxz-3yyz
+    {3, {{{1, 0, 2}, 4.0}, {{3, 0, 0}, -1.0}, {{1, 2, 0}, -1.0}}},   // 4zzx-xxx-yyx
+    {3, {{{0, 1, 2}, 4.0}, {{2, 1, 0}, -1.0}, {{0, 3, 0}, -1.0}}},   // 4zzy-xxy-yyy
+};
+
+int lmax_of(int lmalpha) { return lmalpha == 1 ? 0 : lmalpha == 4 ? 1 : lmalpha == 9 ? 2 : 3; }
+
+// 1-D Obara-Saika overlap table s[i][j], i <= li, j <= lj (unit prefactor).
+void os_1d(double pa, double pb, double inv2z, int li, int lj, double s[6][6]) {
+  s[0][0] = 1.0;
+  for (int i = 0; i <= li; ++i) {
+    if (i > 0) {
+      s[i][0] = pa * s[i - 1][0] + (i > 1 ? (i - 1) * inv2z * s[i - 2][0] : 0.0);
+    }
+    for (int j = 1; j <= lj; ++j) {
+      double v = pb * s[i][j - 1];
+      if (i > 0) v += i * inv2z * s[i - 1][j - 1];
+      if (j > 1) v += (j - 1) * inv2z * s[i][j - 2];
+      s[i][j] = v;
+    }
+  }
+}
+
+// Combine Cartesian values into the sh block (lm1 <= n1, lm2 <= n2).
+template <class F>
+void cart_to_sh(int n1, int n2, F cart, double* sh /*16x16 col-major*/) {
+  for (int b = 0; b < n2; ++b)
+    for (int a = 0; a < n1; ++a) {
+      double v = 0.0;
+      for (int p = 0; p < kHarm[a].n; ++p)
+        for (int q = 0; q < kHarm[b].n; ++q)
+          v += kHarm[a].m[p].c * kHarm[b].m[q].c * cart(kHarm[a].m[p].e, kHarm[b].m[q].e);
+      sh[b * 16 + a] = v;
+    }
+}
+
+// overlap2CIntg / kinetic2CIntg / electron3CIntg equivalents.
+void prim_overlap(double a1, double a2, const double* A, const double* B,
+                  int lma1, int lma2, double* sh) {
+  const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
+  const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
+  double d2 = 0, s[3][6][6];
+  for (int c = 0; c < 3; ++c) {
+    double P = (a1 * A[c] + a2 * B[c]) / z;
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    os_1d(P - A[c], P - B[c], inv2z, l1, l2, s[c]);
+  }
+  const double pref = std::pow(kPi / z, 1.5) * std::exp(-xi * d2);
+  cart_to_sh(lma1, lma2, [&](const int* ea, const int* eb) {
+    return pref * s[0][ea[0]][eb[0]] * s[1][ea[1]][eb[1]] * s[2][ea[2]][eb[2]];
+  }, sh);
+}
+
+// Kinetic energy by the three-dimensional Obara-Saika kinetic recurrence
+//   (a+1_i|T|b) = PA_i (a|T|b) + [N_i(a) (a-1_i|T|b) + N_i(b) (a|T|b-1_i)]/(2 zeta)
+//                 + 2 xi [ (a+1_i|b) - N_i(a)/(2 a1) (a-1_i|b) ]
+// (and the same on b with PB, a2) from (0|T|0) = xi (3 - 2 xi |AB|^2) (0|0),
+// lowering along the last non-zero Cartesian direction.
+void prim_kinetic(double a1, double a2, const double* A, const double* B,
+                  int lma1, int lma2, double* sh) {
+  const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
+  const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
+  double d2 = 0, s[3][6][6], PA[3], PB[3];
+  for (int c = 0; c < 3; ++c) {
+    double P = (a1 * A[c] + a2 * B[c]) / z;
+    PA[c] = P - A[c];
+    PB[c] = P - B[c];
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    os_1d(PA[c], PB[c], inv2z, l1, l2, s[c]);
+  }
+  const double pref = std::pow(kPi / z, 1.5) * std::exp(-xi * d2);
+  // Cartesian lists |e| <= l in the order s; x y z; xx yy zz xy xz yz; ...
+  std::vector<std::array<int, 3>> ca, cb;
+  auto fill = [](int L, std::vector<std::array<int, 3>>& v) {
+    for (int n = 0; n <= L; ++n)
+      for (int x = n; x >= 0; --x)
+        for (int y = n - x; y >= 0; --y) v.push_back({x, y, n - x - y});
+  };
+  fill(l1, ca);
+  fill(l2, cb);
+  auto idx = [](const std::vector<std::array<int, 3>>& v, int x, int y, int zz) {
+    for (size_t q = 0; q < v.size(); ++q)
+      if (v[q][0] == x && v[q][1] == y && v[q][2] == zz) return (int)q;
+    return -1;
+  };
+  const size_t N1 = ca.size(), N2 = cb.size();
+  std::vector<double> S(N1 * N2), Tm(N1 * N2);
+  for (size_t a = 0; a < N1; ++a)
+    for (size_t b = 0; b < N2; ++b)
+      S[a * N2 + b] = pref * s[0][ca[a][0]][cb[b][0]] * s[1][ca[a][1]][cb[b][1]] *
+                      s[2][ca[a][2]][cb[b][2]];
+  Tm[0] = xi * (3.0 - 2.0 * xi * d2) * pref;
+  for (size_t b = 1; b < N2; ++b) {
+    int i = cb[b][2] ? 2 : cb[b][1] ? 1 : 0;
+    std::array<int, 3> bp = cb[b];
+    bp[i]--;
+    int jb = idx(cb, bp[0], bp[1], bp[2]);
+    double v = PB[i] * Tm[jb] + 2.0 * xi * S[b];
+    if (bp[i] > 0) {
+      std::array<int, 3> bq = bp;
+      bq[i]--;
+      int jq = idx(cb, bq[0], bq[1], bq[2]);
+      v += bp[i] * inv2z * Tm[jq] - 2.0 * xi * bp[i] / (2.0 * a2) * S[jq];
+    }
+    Tm[b] = v;
+  }
+  for (size_t a = 1; a < N1; ++a) {
+    int i = ca[a][2] ? 2 : ca[a][1] ? 1 : 0;
+    std::array<int, 3> ap = ca[a];
+    ap[i]--;
+    int ja = idx(ca, ap[0], ap[1], ap[2]);
+    int jaa = -1;
+    if (ap[i] > 0) {
+      std::array<int, 3> aq = ap;
+      aq[i]--;
+      jaa = idx(ca, aq[0], aq[1], aq[2]);
+    }
+    for (size_t b = 0; b < N2; ++b) {
+      double v = PA[i] * Tm[ja * N2 + b] + 2.0 * xi * S[a * N2 + b];
+      if (jaa >= 0) v += ap[i] * inv2z * Tm[jaa * N2 + b] - 2.0 * xi * ap[i] / (2.0 * a1) * S[jaa * N2 + b];
+      if (cb[b][i] > 0) {
+        std::array<int, 3> bq = cb[b];
+        bq[i]--;
+        v += cb[b][i] * inv2z * Tm[ja * N2 + idx(cb, bq[0], bq[1], bq[2])];
+      }
+      Tm[a * N2 + b] = v;
+    }
+  }
+  cart_to_sh(lma1, lma2, [&](const int* ea, const int* eb) {
+    return Tm[idx(ca, ea[0], ea[1], ea[2]) * N2 + idx(cb, eb[0], eb[1], eb[2])];
+  }, sh);
+}
+
+void prim_elec3c(double a1, double a2, double a3, const double* A, const double* B,
+                 const double* Cc, int lma1, int lma2, double* sh) {
+  const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
+  const double z = a1 + a2, z3 = z + a3, inv2z3 = 1.0 / (2.0 * z3), xi = a1 * a2 / z;
+  double d2 = 0, pc2 = 0, s[3][6][6];
+  for (int c = 0; c < 3; ++c) {
+    double P = (a1 * A[c] + a2 * B[c]) / z;
+    double G = (a1 * A[c] + a2 * B[c] + a3 * Cc[c]) / z3;
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    pc2 += (P - Cc[c]) * (P - Cc[c]);
+    os_1d(G - A[c], G - B[c], inv2z3, l1, l2, s[c]);
+  }
+  const double pref = std::pow(kPi / z3, 1.5) * std::exp(-xi * d2 - (z * a3 / z3) * pc2);
+  cart_to_sh(lma1, lma2, [&](const int* ea, const int* eb) {
+    return pref * s[0][ea[0]][eb[0]] * s[1][ea[1]][eb[1]] * s[2][ea[2]][eb[2]];
+  }, sh);
+}
+
+// Boys function F_0..F_6 in the formulation of the reference
+// (gaussIntegrals.f90:16080-16221): for T <= 0.1 (a binary32 literal there)
+// the truncated series 1/2 e^{-T} Gamma(N+1/2) sum_{i<7} T^i/Gamma(N+i+3/2),
+// whose Gamma values the reference's gfortran build holds in binary32; above
+// it the closed forms in erf(sqrt T).
+void boys_reference(double T, double F[7]) {
+  const double thr = (double)0.1f;
+  const double eT = std::exp(-T);
+  if (T <= thr) {
+    double g[14];
+    for (int k = 0; k < 14; ++k) g[k] = (double)(float)std::tgamma(k + 0.5);
+    for (int N = 0; N < 7; ++N) {
+      double acc = 1.0 / g[N + 1];
+      double tp = 1.0;
+      for (int i = 1; i < 7; ++i) { tp *= T; acc += tp / g[N + 1 + i]; }
+      F[N] = 0.5 * eT * g[N] * acc;
+    }
+    return;
+  }
+  const double rt = std::sqrt(T), erfv = std::erf(rt), sp = std::sqrt(kPi);
+  // F_n = (2n-1)!!/2^(n+1) [ sqrt(pi) erf(sqrt T)/T^(n+1/2)
+  //                          - e^-T sum_{k<n} 2^(k+1)/((2k+1)!! T^(n-k)) ]
+  for (int n = 0; n < 7; ++n) {
+    double dfn = 1.0;
+    for (int q = 2 * n - 1; q > 1; q -= 2) dfn *= q;
+    double sum = 0.0, dfk = 1.0;
+    for (int k = 0; k < n; ++k) {
+      if (k > 0) dfk *= (2 * k + 1);
+      sum += std::pow(2.0, k + 1) / (dfk * std::pow(T, n - k));
+    }
+    F[n] = dfn / std::pow(2.0, n + 1) * (sp * erfv / std::pow(T, n + 0.5) - eT * sum);
+  }
+}
+
+// nuclear3CIntg equivalent: OS three-index recursion with auxiliary order m,
+// memoised on (a, b, m).
+struct NucRec {
+  double GA[3], GB[3], GC[3], inv2z3, F0[9];
+  std::map<uint64_t, double> memo;
+  static uint64_t key(const int* a, const int* b, int m) {
+    uint64_t k = 0;
+    for (int c = 0; c < 3; ++c) k = k * 8 + a[c];
+    for (int c = 0; c < 3; ++c) k = k * 8 + b[c];
+    return k * 16 + m;
+  }
+  double eval(const int* a, const int* b, int m) {
+    if (a[0] < 0 || a[1] < 0 || a[2] < 0 || b[0] < 0 || b[1] < 0 || b[2] < 0) return 0.0;
+    if (!a[0] && !a[1] && !a[2] && !b[0] && !b[1] && !b[2]) return F0[m];
+    uint64_t k = key(a, b, m);
+    auto it = memo.find(k);
+    if (it != memo.end()) return it->second;
+    double v;
+    int c = -1;
+    for (int q = 0; q < 3; ++q) if (a[q] > 0) { c = q; break; }
+    if (c >= 0) {  // lower a along c
+      int am[3] = {a[0], a[1], a[2]}; am[c]--;
+      int amm[3] = {am[0], am[1], am[2]}; amm[c]--;
+      int bm[3] = {b[0], b[1], b[2]}; bm[c]--;
+      v = GA[c] * eval(am, b, m) - GC[c] * eval(am, b, m + 1);
+      if (am[c] > 0) v += am[c] * inv2z3 * (eval(amm, b, m) - eval(amm, b, m + 1));
+      if (b[c] > 0) v += b[c] * inv2z3 * (eval(am, bm, m) - eval(am, bm, m + 1));
+    } else {
+      for (int q = 0; q < 3; ++q) if (b[q] > 0) { c = q; break; }
+      int bm[3] = {b[0], b[1], b[2]}; bm[c]--;
+      int bmm[3] = {bm[0], bm[1], bm[2]}; bmm[c]--;
+      v = GB[c] * eval(a, bm, m) - GC[c] * eval(a, bm, m + 1);
+      if (bm[c] > 0) v += bm[c] * inv2z3 * (eval(a, bmm, m) - eval(a, bmm, m + 1));
+    }
+    memo[k] = v;
+    return v;
+  }
+};
+
+void prim_nuclear(double a1, double a2, double a3, const double* A, const double* B,
+                  const double* Cc, int lma1, int lma2, double* sh) {
+  NucRec r;
+  const double z = a1 + a2, z3 = z + a3;
+  r.inv2z3 = 1.0 / (2.0 * z3);
+  double gc2 = 0, e = 0;
+  for (int c = 0; c < 3; ++c) {
+    double G = (a1 * A[c] + a2 * B[c] + a3 * Cc[c]) / z3;
+    r.GA[c] = G - A[c]; r.GB[c] = G - B[c]; r.GC[c] = G - Cc[c];
+    gc2 += r.GC[c] * r.GC[c];
+    double d1 = A[c] - B[c], d2 = A[c] - Cc[c], d3 = B[c] - Cc[c];
+    e += a1 * a2 * d1 * d1 + a1 * a3 * d2 * d2 + a2 * a3 * d3 * d3;
+  }
+  double F[7];
+  boys_reference(z3 * gc2, F);
+  const double pre = 2.0 * (kPi / z3) * std::exp(-e / z3);
+  for (int m = 0; m < 7; ++m) r.F0[m] = F[m] * pre;
+  r.F0[7] = r.F0[8] = 0.0;
+  cart_to_sh(lma1, lma2, [&](const int* ea, const int* eb) {
+    return r.eval(ea, eb, 0);
+  }, sh);
+}
+
+// ---------------------------------------------------------------------------
+// System set-up
+// ---------------------------------------------------------------------------
+struct TypeInfo {
+  int element = 0, nalpha = 0, nvale = 0, ncore = 0, nstates = 0;
+  double alphas[OLC_MAX_ALPHAS] = {};
+  int lmAlpha[OLC_MAX_ALPHAS] = {};
+  int lmIndex[OLC_MAX_STATES] = {};
+  double basis[OLC_MAX_ALPHAS][OLC_MAX_STATES] = {};  // basis(alpha, state)
+};
+
+const double kAngNorm[16] = {
+    0.2820947917738782, 0.4886025119029199, 0.4886025119029199, 0.4886025119029199,
+    1.0925484305920790, 1.0925484305920790, 1.0925484305920790, 0.5462742152960396,
+    0.3153915652525200, 2.8906114426405543, 1.4453057213202771, 0.5900435899266435,
+    0.5900435899266435, 0.3731763325901154, 0.4570457994644657, 0.4570457994644657};
+
+struct Oracle {
+  double rv[3][3];  // rv[abc][xyz]
+  double recip[3][3], invReal[3][3];
+  double T;  // logBasisFnThresh
+  std::vector<double> cellSize;   // |R|^2 sorted
+  std::vector<double> cellDim;    // 3 per cell
+  int nNearCells = 0;
+  std::vector<TypeInfo> types;
+  int nsites = 0;
+  std::vector<int> siteType, cumVale, cumCore;
+  std::vector<double> sitePos;
+  int valeDim = 0, coreDim = 0;
+  // potential
+  std::vector<olc_pot_type_t> pots;
+  std::vector<int> potSiteType;
+  std::vector<double> potSitePos;
+  std::vector<int> potFirst, potMult, potCumAlpha;
+  int potDim = 0;
+  // k-points
+  int nk = 0;
+  std::vector<double> kxyz;
+  // screening tables keyed by element
+  int nElem = 0;
+  std::vector<std::vector<double>> elemAlpha, elemPotAlpha;
+  std::vector<double> elemNucAlpha;
+
+  double alphaDist(int a1, int a2, int e1, int e2) const {
+    // alphaDist(l,k,j,i) = T / alpha(k,i) / alphaCenter(l,k,j,i),
+    // alphaCenter = alpha(l,j)/(alpha(l,j)+alpha(k,i)); l <- (a1,e1), k <- (a2,e2)
+    double al = elemAlpha[e1][a1], ak = elemAlpha[e2][a2];
+    double center = al / (al + ak);
+    return T / ak / center;
+  }
+  double alphaCenter(int a1, int a2, int e1, int e2) const {
+    double al = elemAlpha[e1][a1], ak = elemAlpha[e2][a2];
+    return al / (al + ak);
+  }
+  double alphaNucDist(int a1, int a2, int ek, int e1, int e2) const {
+    double am = elemAlpha[e1][a1], al = elemAlpha[e2][a2], an = elemNucAlpha[ek];
+    return T * (am + al + an) / (am + al) / an;
+  }
+  double alphaPotDist(int a1, int a2, int pa, int e1, int e2, int ep) const {
+    double an = elemAlpha[e1][a1], am = elemAlpha[e2][a2], ap = elemPotAlpha[ep][pa];
+    return T * (an + am + ap) / (an + am) / ap;
+  }
+
+  void findLatticeVector(const double* v, double* L) const {
+    double base[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i) {
+      double ex = 0;
+      for (int c = 0; c < 3; ++c) ex += v[c] * invReal[i][c];
+      double r = (double)(long long)(std::fabs(ex) + 0.5);
+      if (ex < 0) r = -r;
+      for (int c = 0; c < 3; ++c) base[c] += rv[i][c] * r;
+    }
+    double best = 0;
+    for (int c = 0; c < 3; ++c) best += (v[c] - base[c]) * (v[c] - base[c]);
+    int bi = -1;
+    for (int n = 1; n < nNearCells; ++n) {
+      double d = 0;
+      for (int c = 0; c < 3; ++c) {
+        double x = v[c] - base[c] - cellDim[3 * n + c];
+        d += x * x;
+      }
+      if (d < best) { best = d; bi = n; }
+    }
+    for (int c = 0; c < 3; ++c) L[c] = base[c] + (bi >= 0 ? cellDim[3 * bi + c] : 0.0);
+  }
+
+  std::string err;
+
+  int setup(const olc_system_t* s) {
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 3; ++c) rv[i][c] = s->real_vectors[i * 3 + c];
+    // getRecipCellVectors (lattice.f90:180-215)
+    double vol = 0;
+    for (int i = 0; i < 3; ++i) {
+      int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+      for (int j = 0; j < 3; ++j) {
+        int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        recip[i][j] = rv[i1][j1] * rv[i2][j2] - rv[i1][j2] * rv[i2][j1];
+      }
+    }
+    vol = 0;
+    for (int j = 0; j < 3; ++j) vol += recip[0][j] * rv[0][j];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        recip[i][j] = 2.0 * kPi * recip[i][j] / vol;
+        invReal[i][j] = recip[i][j] / (2.0 * kPi);
+      }
+    T = -std::log(s->basis_fn_thresh);
+    // types and basis (basis.f90:55-243)
+    double minAtomicAlpha = 100.0, minPotAlpha = 10000.0;
+    nElem = 0;
+    types.resize(s->num_atom_types);
+    for (int t = 0; t < s->num_atom_types; ++t) {
+      const olc_atom_type_t& at = s->atom_types[t];
+      TypeInfo& ti = types[t];
+      ti.element = at.element - 1;
+      nElem = std::max(nElem, at.element);
+      ti.nalpha = at.num_orb_alphas[0];
+      for (int a = 0; a < ti.nalpha; ++a) ti.alphas[a] = at.alphas[a];
+      minAtomicAlpha = std::min(minAtomicAlpha, at.alphas[0]);
+      for (int a = 0; a < ti.nalpha; ++a) {
+        int j = a + 1;
+        ti.lmAlpha[a] = (j <= at.num_orb_alphas[3]) ? 16 : (j <= at.num_orb_alphas[2]) ? 9
+                        : (j <= at.num_orb_alphas[1]) ? 4 : 1;
+      }
+      int m = 0;
+      int nrad = at.num_vale_radial + at.num_core_radial;
+      for (int r = 0; r < nrad; ++r) {
+        int l = at.radial_l[r];
+        int na = at.num_orb_alphas[l];
+        for (int k = 1; k <= 2 * l + 1; ++k) {
+          if (m >= OLC_MAX_STATES) { err = "too many states"; return OLC_ERR_ARG; }
+          ti.lmIndex[m] = l * l + k;
+          for (int a = 0; a < na; ++a)
+            ti.basis[a][m] = at.radial_coeff[r][a] * kAngNorm[l * l + k - 1];
+          ++m;
+        }
+        if (r + 1 == at.num_vale_radial) ti.nvale = m;
+      }
+      if (at.num_vale_radial == 0) ti.nvale = 0;
+      ti.nstates = m;
+      ti.ncore = m - ti.nvale;
+    }
+    pots.assign(s->pot_types, s->pot_types + s->num_pot_types);
+    for (auto& p : pots) {
+      minPotAlpha = std::min(minPotAlpha, p.alphas[0]);
+      nElem = std::max(nElem, p.element);
+    }
+    // elements (gaussRelations.f90: first type of each element)
+    elemAlpha.assign(nElem, {});
+    elemPotAlpha.assign(nElem, {});
+    elemNucAlpha.assign(nElem, 0.0);
+    for (auto& ti : types)
+      if (elemAlpha[ti.element].empty()) elemAlpha[ti.element].assign(ti.alphas, ti.alphas + ti.nalpha);
+    for (auto& p : pots) {
+      if (elemPotAlpha[p.element - 1].empty())
+        elemPotAlpha[p.element - 1].assign(p.alphas, p.alphas + p.num_alphas);
+      if (elemNucAlpha[p.element - 1] == 0.0) elemNucAlpha[p.element - 1] = p.nuc_alpha;
+    }
+    // sites
+    nsites = s->num_atom_sites;
+    siteType.assign(s->site_type, s->site_type + nsites);
+    sitePos.assign(s->site_pos, s->site_pos + 3 * nsites);
+    cumVale.resize(nsites);
+    cumCore.resize(nsites);
+    valeDim = coreDim = 0;
+    for (int i = 0; i < nsites; ++i) {
+      cumVale[i] = valeDim;
+      cumCore[i] = coreDim;
+      valeDim += types[siteType[i]].nvale;
+      coreDim += types[siteType[i]].ncore;
+    }
+    potSiteType.assign(s->pot_site_type, s->pot_site_type + s->num_pot_sites);
+    potSitePos.assign(s->pot_site_pos, s->pot_site_pos + 3 * s->num_pot_sites);
+    potFirst.assign(pots.size(), -1);
+    potMult.assign(pots.size(), 0);
+    for (int i = 0; i < (int)potSiteType.size(); ++i) {
+      int t = potSiteType[i];
+      if (potFirst[t] < 0) potFirst[t] = i;
+      potMult[t]++;
+    }
+    potCumAlpha.resize(pots.size());
+    potDim = 0;
+    for (size_t t = 0; t < pots.size(); ++t) { potCumAlpha[t] = potDim; potDim += pots[t].num_alphas; }
+    // initializeLattice (lattice.f90:300-432)
+    double negl = T * std::max(2.0 / minAtomicAlpha, 1.0 / minPotAlpha + 0.5 / minAtomicAlpha);
+    double maxSq = 0;
+    for (int i = 0; i < 3; ++i) {
+      double sq = 0;
+      for (int c = 0; c < 3; ++c) sq += rv[i][c] * rv[i][c];
+      maxSq = std::max(maxSq, sq);
+    }
+    negl = negl + 0.75 * maxSq + std::sqrt(3.0 * maxSq * negl);
+    negl = std::max(negl, 2.0 * T / minAtomicAlpha);
+    int reps[3];
+    for (int i = 0; i < 3; ++i) {
+      double len = std::sqrt(rv[i][0] * rv[i][0] + rv[i][1] * rv[i][1] + rv[i][2] * rv[i][2]);
+      reps[i] = 2 * (int)std::ceil(std::sqrt(negl) / len) + 1;
+    }
+    double shifts[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 3; ++c) shifts[c] += rv[i][c];
+    std::vector<std::pair<double, int>> order;
+    std::vector<double> dims;
+    for (int i = 1; i <= reps[0]; ++i)
+      for (int j = 1; j <= reps[1]; ++j)
+        for (int k = 1; k <= reps[2]; ++k) {
+          int rep[3] = {i - (1 + reps[0]) / 2, j - (1 + reps[1]) / 2, k - (1 + reps[2]) / 2};
+          double d[3] = {0, 0, 0};
+          for (int l = 0; l < 3; ++l)
+            for (int c = 0; c < 3; ++c) d[c] += rv[l][c] * rep[l];
+          double sq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          if (sq > negl) {
+            // cellBorderCheck: seven corners of the cell (lattice.f90:676-747)
+            static const int seq[7][2] = {{0, 1}, {1, 1}, {0, -1}, {2, 1}, {0, 1}, {1, -1}, {0, -1}};
+            double t[3] = {d[0], d[1], d[2]};
+            bool in = false;
+            for (int q = 0; q < 7 && !in; ++q) {
+              t[seq[q][0]] += seq[q][1] * shifts[seq[q][0]];
+              if (t[0] * t[0] + t[1] * t[1] + t[2] * t[2] < negl) in = true;
+            }
+            if (!in) continue;
+          }
+          order.push_back({sq, (int)dims.size() / 3});
+          dims.insert(dims.end(), d, d + 3);
+        }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+                       return a.first < b.first;
+                     });
+    cellSize.resize(order.size());
+    cellDim.resize(3 * order.size());
+    for (size_t n = 0; n < order.size(); ++n) {
+      cellSize[n] = order[n].first;
+      for (int c = 0; c < 3; ++c) cellDim[3 * n + c] = dims[3 * order[n].second + c];
+    }
+    // neighbourhood searched by findLatticeVector: all cells with
+    // |R|^2 <= 3 * (longest cell vector)^2
+    nNearCells = 0;
+    while (nNearCells < (int)cellSize.size() && cellSize[nNearCells] <= 3.0 * maxSq * (1 + 1e-12))
+      ++nNearCells;
+    // k-points to xyz (kpoints.f90:251-281)
+    nk = s->num_kpoints;
+    kxyz.resize(3 * nk);
+    for (int q = 0; q < nk; ++q)
+      for (int c = 0; c < 3; ++c) {
+        double v = 0;
+        for (int i = 0; i < 3; ++i) v += s->kpoints_abc[3 * q + i] * recip[i][c];
+        kxyz[3 * q + c] = v;
+      }
+    return OLC_OK;
+  }
+
+  // -------------------------------------------------------------------------
+  // integral drivers
+  // -------------------------------------------------------------------------
+  // Third-centre sums (nuclearPE / electronicPE).  Returns contrib.
+  bool third_centre(int op, int a1, int a2, int e1, int e2, int lma1, int lma2,
+                    double sep, const double* A, const double* Bs, double al1, double al2,
+                    int potType, int potAlpha, double* out) {
+    double oc[3];
+    double cen = alphaCenter(a1, a2, e1, e2);
+    for (int c = 0; c < 3; ++c) oc[c] = cen * (A[c] - Bs[c]) + Bs[c];
+    for (int b = 0; b < 16; ++b)
+      for (int a = 0; a < 16; ++a) out[b * 16 + a] = 0.0;
+    bool contrib = false;
+    double sh[256];
+    auto site_loop = [&](int m, double a3, double zfac, double tad) {
+      const double* pp = &potSitePos[3 * m];
+      double v[3] = {oc[0] - pp[0], oc[1] - pp[1], oc[2] - pp[2]};
+      double L2[3];
+      findLatticeVector(v, L2);
+      double cov[3] = {v[0] - L2[0], v[1] - L2[1], v[2] - L2[2]};
+      double cos2 = cov[0] * cov[0] + cov[1] * cov[1] + cov[2] * cov[2];
+      if (cos2 > tad) return;
+      contrib = true;
+      double maxR2 = cos2 + tad + 2.0 * std::sqrt(cos2 * tad);
+      for (size_t n = 0; n < cellSize.size(); ++n) {
+        if (cellSize[n] > maxR2) break;
+        double x = cov[0] - cellDim[3 * n], y = cov[1] - cellDim[3 * n + 1], z = cov[2] - cellDim[3 * n + 2];
+        if (x * x + y * y + z * z > tad) continue;
+        double Cp[3] = {pp[0] + L2[0] + cellDim[3 * n], pp[1] + L2[1] + cellDim[3 * n + 1],
+                        pp[2] + L2[2] + cellDim[3 * n + 2]};
+        if (op == OLC_OP_NUCLEAR) {
+          prim_nuclear(al1, al2, a3, A, Bs, Cp, lma1, lma2, sh);
+          for (int b = 0; b < lma2; ++b)
+            for (int a = 0; a < lma1; ++a) out[b * 16 + a] -= sh[b * 16 + a] * zfac;
+        } else {
+          prim_elec3c(al1, al2, a3, A, Bs, Cp, lma1, lma2, sh);
+          for (int b = 0; b < lma2; ++b)
+            for (int a = 0; a < lma1; ++a) out[b * 16 + a] += sh[b * 16 + a];
+        }
+      }
+    };
+    double frac = 1.0 - sep / alphaDist(a1, a2, e1, e2);
+    if (op == OLC_OP_NUCLEAR) {
+      for (int m = 0; m < (int)potSiteType.size(); ++m) {
+        const olc_pot_type_t& p = pots[potSiteType[m]];
+        if (p.nuc_charge < 1.0e-8) continue;   // smallThresh (constants.f90:49)
+        double tad = frac * alphaNucDist(a1, a2, p.element - 1, e1, e2);
+        site_loop(m, p.nuc_alpha, p.nuc_charge, tad);
+      }
+    } else {
+      const olc_pot_type_t& p = pots[potType];
+      double tad = frac * alphaPotDist(a1, a2, potAlpha, e1, e2, p.element - 1);
+      for (int m = 0; m < potMult[potType]; ++m)
+        site_loop(potFirst[potType] + m, p.alphas[potAlpha], 0.0, tad);
+    }
+    return contrib;
+  }
+
+  // One operator pass; outputs complex arrays (column-major, full storage).
+  int run_operator(int op, int term, cplx* vv, cplx* cv, cplx* cc) {
+    int potType = -1, potAlpha = -1;
+    if (op == OLC_OP_ELECPOT) {
+      for (size_t t = 0; t < pots.size(); ++t)
+        if (term >= potCumAlpha[t] && term < potCumAlpha[t] + pots[t].num_alphas) {
+          potType = (int)t;
+          potAlpha = term - potCumAlpha[t];
+        }
+      if (potType < 0) { err = "potential term out of range"; return OLC_ERR_ARG; }
+    }
+    const size_t nv = valeDim, nc = coreDim;
+    std::fill(vv, vv + nv * nv * nk, cplx(0, 0));
+    if (cv) std::fill(cv, cv + nc * nv * nk, cplx(0, 0));
+    if (cc) std::fill(cc, cc + nc * nc * nk, cplx(0, 0));
+    const int MS = OLC_MAX_STATES;
+    std::vector<cplx> cur((size_t)MS * MS * nk);
+    std::vector<double> pairX(16 * OLC_MAX_ALPHAS * MS);
+    double block[OLC_MAX_STATES * OLC_MAX_STATES];
+    double sh[256];
+    for (int i = 0; i < nsites; ++i) {
+      const TypeInfo& t1 = types[siteType[i]];
+      const double* A = &sitePos[3 * i];
+      for (int j = i; j < nsites; ++j) {
+        const TypeInfo& t2 = types[siteType[j]];
+        const double* B = &sitePos[3 * j];
+        int e1 = t1.element, e2 = t2.element;
+        double dv[3] = {A[0] - B[0], A[1] - B[1], A[2] - B[2]};
+        double L[3];
+        findLatticeVector(dv, L);
+        double sepSq = 0;
+        for (int c = 0; c < 3; ++c) sepSq += (dv[c] - L[c]) * (dv[c] - L[c]);
+        double negl = alphaDist(0, 0, e1, e2);
+        if (sepSq > negl) continue;
+        double maxR = sepSq + negl + 2.0 * std::sqrt(sepSq * negl);
+        if (maxR > cellSize.back()) {
+          err = "More lattice points needed for this atom overlap pair";
+          return OLC_ERR_LATTICE;
+        }
+        const int M1 = t1.nstates, M2 = t2.nstates;
+        std::fill(cur.begin(), cur.end(), cplx(0, 0));
+        for (size_t k = 0; k < cellSize.size(); ++k) {
+          if (cellSize[k] > maxR) break;
+          double Bs[3];
+          for (int c = 0; c < 3; ++c) Bs[c] = B[c] + L[c] + cellDim[3 * k + c];
+          double sep = 0;
+          for (int c = 0; c < 3; ++c) sep += (A[c] - Bs[c]) * (A[c] - Bs[c]);
+          if (sep > negl) continue;
+          std::fill(pairX.begin(), pairX.end(), 0.0);
+          int maxA1 = 0;
+          // alpha-pair traversal (integrals.F90:312-416)
+          int nmin = std::min(t1.nalpha, t2.nalpha);
+          for (int l = 0; l < nmin; ++l) {
+            if (alphaDist(l, l, e1, e2) < sep) break;
+            int mode = 0;
+            int ai[2] = {l, l};
+            while (true) {
+              if (mode == 1) {
+                ai[0]++;
+                if (ai[0] >= t1.nalpha) { mode = 2; ai[0] = l; continue; }
+              } else if (mode == 2) {
+                ai[1]++;
+                if (ai[1] >= t2.nalpha) break;
+              }
+              if (alphaDist(ai[0], ai[1], e1, e2) < sep) {
+                if (mode == 1) { mode = 2; ai[0] = l; continue; }
+                break;
+              }
+              if (mode == 0) mode = 1;
+              int lma1 = t1.lmAlpha[ai[0]], lma2 = t2.lmAlpha[ai[1]];
+              double al1 = t1.alphas[ai[0]], al2 = t2.alphas[ai[1]];
+              bool contrib = true;
+              if (op == OLC_OP_OVERLAP) prim_overlap(al1, al2, A, Bs, lma1, lma2, sh);
+              else if (op == OLC_OP_KINETIC) prim_kinetic(al1, al2, A, Bs, lma1, lma2, sh);
+              else contrib = third_centre(op, ai[0], ai[1], e1, e2, lma1, lma2, sep, A, Bs,
+                                          al1, al2, potType, potAlpha, sh);
+              if (contrib) {
+                for (int m = 0; m < M2; ++m) {
+                  int lm2 = t2.lmIndex[m];
+                  if (lm2 > lma2) continue;   // basis(alpha2, m) == 0 there
+                  double c2 = t2.basis[ai[1]][m];
+                  double* px = &pairX[(size_t)(m * OLC_MAX_ALPHAS + ai[0]) * 16];
+                  for (int a = 0; a < lma1; ++a) px[a] += sh[(lm2 - 1) * 16 + a] * c2;
+                }
+                maxA1 = std::max(maxA1, ai[0] + 1);
+              }
+            }
+          }
+          if (op == OLC_OP_OVERLAP && maxA1 == 0) continue;
+          // multWithBasisFn1 (intgSaving.F90:56-89)
+          for (int m2 = 0; m2 < M2; ++m2)
+            for (int m1 = 0; m1 < M1; ++m1) {
+              double s = 0;
+              int lm1 = t1.lmIndex[m1];
+              for (int a = 0; a < maxA1; ++a)
+                s += t1.basis[a][m1] * pairX[(size_t)(m2 * OLC_MAX_ALPHAS + a) * 16 + lm1 - 1];
+              block[m2 * MS + m1] = s;
+            }
+          // applyPhaseFactors (intgSaving.F90:95-147)
+          for (int q = 0; q < nk; ++q) {
+            double kr = kxyz[3 * q] * cellDim[3 * k] + kxyz[3 * q + 1] * cellDim[3 * k + 1] +
+                        kxyz[3 * q + 2] * cellDim[3 * k + 2];
+            cplx ph(std::cos(kr), std::sin(kr));
+            cplx* cp = &cur[(size_t)q * MS * MS];
+            for (int m2 = 0; m2 < M2; ++m2)
+              for (int m1 = 0; m1 < M1; ++m1) cp[m2 * MS + m1] += ph * block[m2 * MS + m1];
+          }
+        }
+        // kPointLatticeOriginShift (intgSaving.F90:150-198)
+        for (int q = 0; q < nk; ++q) {
+          double kl = kxyz[3 * q] * L[0] + kxyz[3 * q + 1] * L[1] + kxyz[3 * q + 2] * L[2];
+          if (kl != 0.0) {
+            cplx ph(std::cos(kl), std::sin(kl));
+            cplx* cp = &cur[(size_t)q * MS * MS];
+            for (int m2 = 0; m2 < M2; ++m2)
+              for (int m1 = 0; m1 < M1; ++m1) cp[m2 * MS + m1] = ph * cp[m2 * MS + m1];
+          }
+        }
+        save_pair(i, j, cur.data(), vv, cv, cc);
+      }
+    }
+    return OLC_OK;
+  }
+
+  // saveCurrentPair and helpers (intgSaving.F90:201-505)
+  void save_pair(int i, int j, const cplx* cur, cplx* vv, cplx* cv, cplx* cc) {
+    const int MS = OLC_MAX_STATES;
+    const TypeInfo& t1 = types[siteType[i]];
+    const TypeInfo& t2 = types[siteType[j]];
+    const size_t nv = valeDim, nc = coreDim;
+    int vi1 = cumVale[i], vi2 = cumVale[j], vn1 = t1.nvale, vn2 = t2.nvale;
+    int ci1 = cumCore[i], ci2 = cumCore[j], cn1 = t1.ncore, cn2 = t2.ncore;
+    for (int q = 0; q < nk; ++q) {
+      const cplx* cp = &cur[(size_t)q * MS * MS];
+      cplx* V = vv + (size_t)q * nv * nv;
+      for (int b = 0; b < vn2; ++b)
+        for (int a = 0; a < vn1; ++a) V[(size_t)(vi2 + b) * nv + vi1 + a] = cp[b * MS + a];
+      if (i == j)
+        for (int a = 0; a < vn1; ++a)
+          for (int b = a + 1; b < vn2; ++b) V[(size_t)(vi1 + a) * nv + vi1 + b] = 0.0;
+      if (nc == 0) continue;
+      cplx* CV = cv + (size_t)q * nc * nv;
+      if (cn1)
+        for (int b = 0; b < vn2; ++b)
+          for (int a = 0; a < cn1; ++a) CV[(size_t)(vi2 + b) * nc + ci1 + a] = cp[b * MS + vn1 + a];
+      if (cn2)
+        for (int b = 0; b < vn1; ++b)
+          for (int a = 0; a < cn2; ++a)   // dagger: conj(cur(b, vn2+a))
+            CV[(size_t)(vi1 + b) * nc + ci2 + a] = std::conj(cp[(vn2 + a) * MS + b]);
+      if (!cn1 || !cn2) continue;
+      cplx* CC = cc + (size_t)q * nc * nc;
+      for (int b = 0; b < cn2; ++b)
+        for (int a = 0; a < cn1; ++a) CC[(size_t)(ci2 + b) * nc + ci1 + a] = cp[(vn2 + b) * MS + vn1 + a];
+      if (i != j)
+        for (int b = 0; b < cn1; ++b)
+          for (int a = 0; a < cn2; ++a)
+            CC[(size_t)(ci1 + b) * nc + ci2 + a] = std::conj(cp[(vn2 + a) * MS + vn1 + b]);
+    }
+  }
+
+  // orthoOL / ortho(opCode) + makeValeVale with packing (intgOrtho.F90:23-187)
+  void ortho_pack(bool isOverlap, cplx* vv, const cplx* cv, const cplx* cc,
+                  const cplx* scv, double* packed) {
+    const size_t nv = valeDim, nc = coreDim;
+    const size_t plen = nv * (nv + 1) / 2;
+    std::vector<cplx> vc(nc * nv);
+    for (int q = 0; q < nk; ++q) {
+      cplx* V = vv + (size_t)q * nv * nv;
+      double* P = packed + (size_t)q * 2 * plen;
+      if (nc == 0) {
+        size_t idx = 0;
+        for (size_t i = 0; i < nv; ++i)
+          for (size_t j = 0; j <= i; ++j, ++idx) {
+            P[2 * idx] = V[i * nv + j].real();
+            P[2 * idx + 1] = V[i * nv + j].imag();
+          }
+        continue;
+      }
+      const cplx* S = scv + (size_t)q * nc * nv;
+      const cplx* O = cv + (size_t)q * nc * nv;
+      const cplx* CCq = cc + (size_t)q * nc * nc;
+      // zherk('U','C', -2) or zher2k('U','C', -1): upper, diagonal made real
+      for (size_t i = 0; i < nv; ++i)
+        for (size_t j = 0; j <= i; ++j) {
+          cplx s(0, 0);
+          if (isOverlap) {
+            for (size_t c = 0; c < nc; ++c) s += std::conj(S[j * nc + c]) * S[i * nc + c];
+            s *= -2.0;
+          } else {
+            for (size_t c = 0; c < nc; ++c)
+              s += std::conj(S[j * nc + c]) * O[i * nc + c] + std::conj(O[j * nc + c]) * S[i * nc + c];
+            s = -s;
+          }
+          if (i == j) V[i * nv + j] = cplx(V[i * nv + j].real() + s.real(), 0.0);
+          else V[i * nv + j] += s;
+        }
+      // coreValeCoreCore: valeCore(c, v) = sum_c' conj(S(c', v)) O_cc(c', c)
+      for (size_t v = 0; v < nv; ++v)
+        for (size_t c = 0; c < nc; ++c) {
+          cplx s(0, 0);
+          for (size_t cp = 0; cp < nc; ++cp) s += std::conj(S[v * nc + cp]) * CCq[c * nc + cp];
+          vc[v * nc + c] = s;
+        }
+      size_t idx = 0;
+      for (size_t i = 0; i < nv; ++i)
+        for (size_t j = 0; j <= i; ++j, ++idx) {
+          cplx s(0, 0);
+          for (size_t c = 0; c < nc; ++c) s += vc[j * nc + c] * S[i * nc + c];
+          V[i * nv + j] += s;
+          double re = V[i * nv + j].real(), im = V[i * nv + j].imag();
+          P[2 * idx] = std::fabs(re) < 1.0e-10 ? 0.0 : re;
+          P[2 * idx + 1] = std::fabs(im) < 1.0e-10 ? 0.0 : im;
+        }
+    }
+  }
+};
+
+thread_local std::string g_err;
+
+}  // namespace
+
+extern "C" {
+
+void* orc_create(const olc_system_t* s) {
+  Oracle* o = new Oracle();
+  if (o->setup(s) != OLC_OK) {
+    g_err = o->err;
+    delete o;
+    return nullptr;
+  }
+  return o;
+}
+
+void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+const char* orc_error(void) { return g_err.c_str(); }
+
+void orc_dims(void* h, int32_t* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  out[0] = o->valeDim;
+  out[1] = o->coreDim;
+  out[2] = o->potDim;
+  out[3] = o->nk;
+  out[4] = (int32_t)o->cellSize.size();
+}
+
+// cells: [ncells*4] = (x, y, z, |R|^2) in the reference's sorted order
+void orc_cells(void* h, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  for (size_t n = 0; n < o->cellSize.size(); ++n) {
+    for (int c = 0; c < 3; ++c) out[4 * n + c] = o->cellDim[3 * n + c];
+    out[4 * n + 3] = o->cellSize[n];
+  }
+}
+
+int orc_operator(void* h, int op, int term, double* vv, double* cv, double* cc) {
+  Oracle* o = static_cast<Oracle*>(h);
+  int st = o->run_operator(op, term, reinterpret_cast<cplx*>(vv), reinterpret_cast<cplx*>(cv),
+                           reinterpret_cast<cplx*>(cc));
+  if (st) g_err = o->err;
+  return st;
+}
+
+void orc_ortho_pack(void* h, int is_overlap, double* vv, const double* cv, const double* cc,
+                    const double* scv, double* packed) {
+  Oracle* o = static_cast<Oracle*>(h);
+  o->ortho_pack(is_overlap != 0, reinterpret_cast<cplx*>(vv), reinterpret_cast<const cplx*>(cv),
+                reinterpret_cast<const cplx*>(cc), reinterpret_cast<const cplx*>(scv), packed);
+}
+
+// Primitive evaluation: kind 1 overlap, 2 kinetic, 3 nuclear, 4 electron3C.
+// in = (a1,a2,a3,A[3],B[3],C[3]); out = sh(16,16) column-major.
+void orc_primitive(int kind, const double* in, const int32_t* lmalpha, double* out) {
+  for (int q = 0; q < 256; ++q) out[q] = 0.0;
+  const double *A = in + 3, *B = in + 6, *Cc = in + 9;
+  switch (kind) {
+    case 1: prim_overlap(in[0], in[1], A, B, lmalpha[0], lmalpha[1], out); break;
+    case 2: prim_kinetic(in[0], in[1], A, B, lmalpha[0], lmalpha[1], out); break;
+    case 3: prim_nuclear(in[0], in[1], in[2], A, B, Cc, lmalpha[0], lmalpha[1], out); break;
+    case 4: prim_elec3c(in[0], in[1], in[2], A, B, Cc, lmalpha[0], lmalpha[1], out); break;
+  }
+}
+
+void orc_boys(double T, double* F) { boys_reference(T, F); }
+
+}  // extern "C"

@@ -1,0 +1,173 @@
+"""ctypes front end of the CPU oracle (oracle/olcao_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline leg of bench.py as the checker, never by the product.
+
+Besides the compiled restatement of the reference loops this module holds the
+eigen-solve leg of the oracle: scipy's LAPACK ``zhegv`` (the routine
+src/olcao/interfaces.F90:105 calls) on the unpacked H(k), S(k).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB: Optional[C.CDLL] = None
+
+OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT = 1, 2, 3, 4
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return os.path.join(_HERE, "_build", "liboracle.so")
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "_build", "liboracle.so")
+        src = os.path.join(_HERE, "olcao_oracle.cpp")
+        if (not os.path.exists(path)) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = C.CDLL(path)
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.c_void_p]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_error.restype = C.c_char_p
+        L.orc_dims.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_cells.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_operator.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]
+        L.orc_operator.restype = C.c_int
+        L.orc_ortho_pack.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 5
+        L.orc_primitive.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_boys.argtypes = [C.c_double, C.c_void_p]
+        _LIB = L
+    return _LIB
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def primitive(kind: int, params: Sequence[float], lmalpha: Sequence[int]) -> np.ndarray:
+    """One primitive sh(16,16) block (column-major in memory, returned [16,16]
+    indexed [row, col])."""
+    inp = np.ascontiguousarray(params, np.float64)
+    lm = np.ascontiguousarray(lmalpha, np.int32)
+    out = np.zeros(256)
+    lib().orc_primitive(kind, _p(inp), _p(lm), _p(out))
+    return out.reshape(16, 16).T
+
+
+def boys(T: float) -> np.ndarray:
+    F = np.zeros(7)
+    lib().orc_boys(float(T), _p(F))
+    return F
+
+
+class Oracle:
+    """One system set up on the CPU (lattice, basis, tables)."""
+
+    def __init__(self, system):
+        self.system = system
+        self._struct = system.to_struct()
+        h = lib().orc_create(C.byref(self._struct))
+        if not h:
+            raise RuntimeError(lib().orc_error().decode())
+        self.h = h
+        d = np.zeros(5, np.int32)
+        lib().orc_dims(h, _p(d))
+        self.vale_dim, self.core_dim, self.pot_dim, self.nk, self.ncells = map(int, d)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros((self.ncells, 4))
+        lib().orc_cells(self.h, _p(out))
+        return out
+
+    def operator(self, op: int, term: int = 0):
+        """Un-orthogonalised (vv, cv, cc) complex arrays, shape [nk, cols, rows]
+        in memory order of the reference's (rows, cols, nk) column-major."""
+        nv, nc, nk = self.vale_dim, self.core_dim, self.nk
+        vv = np.zeros((nk, nv, nv), np.complex128)
+        cv = np.zeros((nk, nv, nc), np.complex128) if nc else None
+        cc = np.zeros((nk, nc, nc), np.complex128) if nc else None
+        st = lib().orc_operator(self.h, op, term, _p(vv), _p(cv), _p(cc))
+        if st:
+            raise RuntimeError(f"oracle status {st}: {lib().orc_error().decode()}")
+        return vv, cv, cc
+
+    def ortho_pack(self, is_overlap: bool, vv, cv, cc, scv) -> np.ndarray:
+        nv, nk = self.vale_dim, self.nk
+        packed = np.zeros((nk, nv * (nv + 1) // 2, 2))
+        vv = vv.copy()
+        lib().orc_ortho_pack(self.h, int(is_overlap), _p(vv), _p(cv), _p(cc),
+                             _p(scv), _p(packed))
+        return packed
+
+    # ---- convenience: the reference's stored integrals ----------------------
+    def packed_operators(self, terms: Optional[Sequence[int]] = None) -> Dict[str, np.ndarray]:
+        """Packed, orthogonalised S, KE, NP and V_j as the reference's
+        OLCAOsetup writes them (integrals.F90 ortho + pack)."""
+        vvS, cvS, ccS = self.operator(OP_OVERLAP)
+        out = {"S": self.ortho_pack(True, vvS, cvS, ccS, cvS)}
+        for name, op in (("KE", OP_KINETIC), ("NP", OP_NUCLEAR)):
+            vv, cv, cc = self.operator(op)
+            out[name] = self.ortho_pack(False, vv, cv, cc, cvS)
+        terms = range(self.pot_dim) if terms is None else terms
+        for j in terms:
+            vv, cv, cc = self.operator(OP_ELECPOT, j)
+            out[f"V{j}"] = self.ortho_pack(False, vv, cv, cc, cvS)
+        return out
+
+
+def assemble(packed: Dict[str, np.ndarray], coeffs: np.ndarray) -> np.ndarray:
+    """secularEqn.F90:128-150 with readPackedMatrixAccum's rule that a zero
+    multiplier adds the term unscaled (matrixSubs.F90:278-282)."""
+    h = packed["NP"].copy()
+    h = h + packed["KE"]
+    for j, c in enumerate(coeffs):
+        v = packed[f"V{j}"]
+        h = h + v if c == 0.0 else h + v * c
+    return h
+
+
+def unpack(packed_k: np.ndarray, n: int) -> np.ndarray:
+    """unpackMatrix with fullFlag=1 (matrixSubs.F90:314-341): Hermitian full."""
+    m = np.zeros((n, n), np.complex128)
+    iu = np.triu_indices(n)
+    # packed order: column i, rows j <= i  -> (j, i)
+    cols = np.concatenate([np.full(i + 1, i) for i in range(n)])
+    rows = np.concatenate([np.arange(i + 1) for i in range(n)])
+    vals = packed_k[:, 0] + 1j * packed_k[:, 1]
+    m[rows, cols] = vals
+    m[cols, rows] = np.conj(vals)
+    m[np.arange(n), np.arange(n)] = packed_k[[(i * (i + 3)) // 2 for i in range(n)], 0]
+    del iu
+    return m
+
+
+def zhegv(h_packed: np.ndarray, s_packed: np.ndarray, n: int, num_states: int):
+    """Eigenvalues/vectors per k with LAPACK zhegv (itype 1, 'V', 'U')."""
+    import scipy.linalg as sl
+    nk = h_packed.shape[0]
+    w = np.zeros((nk, num_states))
+    vecs = np.zeros((nk, n, num_states), np.complex128)
+    for q in range(nk):
+        H = unpack(h_packed[q], n)
+        S = unpack(s_packed[q], n)
+        ev, Z = sl.eigh(H, S, type=1, driver="gv", lower=False)
+        w[q] = ev[:num_states]
+        vecs[q] = Z[:, :num_states]
+    return w, vecs

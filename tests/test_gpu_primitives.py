@@ -1,0 +1,36 @@
+"""Device primitives against the reference's own generated integral code (gpu).
+
+tests/golden/primitives.npz holds sh(16,16) blocks evaluated from
+src/olcao/gaussIntegrals.f90 statement by statement; the CUDA Obara-Saika
+primitives (overlap, kinetic, nuclear with the reference-formulated Boys
+function, three-centre overlap) must reproduce them.
+"""
+
+import numpy as np
+import pytest
+
+
+def _block_err(ref, got, l1, l2):
+    r = ref[:l1, :l2]
+    g = got[:l1, :l2]
+    return np.abs(r - g).max() / max(np.abs(r).max(), 1e-300)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
+def test_device_primitives_match_reference(gpu_lib, golden, kind):
+    from olcao_gb300 import api
+    sel = (golden["kind"] == kind) & (golden["lmalpha"].max(axis=1) <= 9)
+    params = golden["params"][sel]
+    lm = golden["lmalpha"][sel]
+    ref = golden["sh"][sel]
+    got = api.primitive_batch(kind, params, lm)
+    worst = 0.0
+    for i in range(len(params)):
+        e = _block_err(ref[i], got[i], lm[i, 0], lm[i, 1])
+        # near the reference's T = 0.1 Boys switch its closed forms lose
+        # digits to cancellation; both sides carry that rounding
+        tol = 1e-12 if kind != 3 else 1e-9
+        assert e <= tol, f"kind {kind} item {i} lm {lm[i]}: rel err {e:.2e}"
+        worst = max(worst, e)
+    assert worst < 1e-9
