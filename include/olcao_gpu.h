@@ -176,18 +176,55 @@ int olc_solve_zhegv(olc_context_t* ctx, const double* packed_h,
                     const double* packed_s, int num_states,
                     double* eigenvalues, double* vectors, int32_t* info);
 
-/* Set-up of the iteration-invariant parts of the SCF pass: S(k) orthogonalised
- * and factored, and H0 = ortho(KE + NP).  Must precede olc_scf_iteration. */
-int olc_scf_prepare(olc_context_t* ctx, int precision);
+/* How the potential-dependent part of H(k) is produced each iteration. */
+typedef enum {
+  OLC_FORM_FUSED = 0,     /* V = sum_j c_j V_j recomputed from the integrals  */
+  OLC_FORM_STORED = 1     /* V_j kept resident in HBM (OLCAOsetup's stored
+                             integrals) and summed with the coefficients     */
+} olc_form_t;
 
-/* One SCF-iteration pass of the hot path: V = sum_j c_j V_j recomputed from
- * the integrals with the given coefficients, orthogonalised, added to H0,
- * and the generalised eigen-problem solved for all k.  coeffs is a HOST
- * array [pot_dim]; eigenvalues is a HOST or DEVICE array [num_states, nk]
- * (eig_on_device selects).  vectors (DEVICE, may be NULL) as above. */
+/* Flags of olc_scf_iteration. */
+#define OLC_ITER_EIG_DEVICE   1   /* eigenvalues pointer is device memory    */
+#define OLC_ITER_COEFF_DEVICE 2   /* coeffs pointer is device memory         */
+
+/* Set-up of the iteration-invariant parts of the SCF pass: S(k) orthogonalised,
+ * H0 = ortho(KE + NP), and for OLC_FORM_STORED every orthogonalised, packed
+ * V_j.  Must precede olc_scf_iteration. */
+int olc_scf_prepare(olc_context_t* ctx, int precision, int form);
+
+/* One SCF-iteration pass of the hot path (secularEqnAllKP): H(k) built with
+ * the coefficients coeffs[pot_dim] in the prepared form, then the generalised
+ * eigen-problem solved for all k.  eigenvalues[num_states, nk]; vectors
+ * (DEVICE, may be NULL) as for olc_solve_zhegv; flags: OLC_ITER_*. */
 int olc_scf_iteration(olc_context_t* ctx, const double* coeffs, int precision,
-                      int num_states, double* eigenvalues, int eig_on_device,
+                      int num_states, double* eigenvalues, int flags,
                       double* vectors);
+
+/* H(k) and S(k) as the prepared SCF pass builds them, for one k-point, as
+ * full Hermitian complex128 [vale_dim, vale_dim] matrices (host or device
+ * destination): lets a caller hand the secular equation to another solver
+ * or write it out.  coeffs is a HOST array [pot_dim]. */
+int olc_scf_matrices(olc_context_t* ctx, const double* coeffs, int kpoint,
+                     double* h, double* s, int on_device);
+
+/* Stage timing (CUDA events on the context's stream) and kernel counting.
+ * Stages: the integral primitives, the basis contraction, the Bloch sum and
+ * scatter, the orthogonalisation (GEMMs + pack), Hamiltonian assembly, and
+ * the eigen-solve.  olc_profile_read synchronises the stream. */
+typedef enum {
+  OLC_STAGE_PRIMITIVES = 0,
+  OLC_STAGE_CONTRACT = 1,
+  OLC_STAGE_BLOCH = 2,
+  OLC_STAGE_ORTHO = 3,
+  OLC_STAGE_ASSEMBLE = 4,
+  OLC_STAGE_SOLVE = 5,
+  OLC_NUM_STAGES = 6
+} olc_stage_t;
+int olc_profile_enable(olc_context_t* ctx, int on);
+int olc_profile_reset(olc_context_t* ctx);
+int olc_profile_read(olc_context_t* ctx, int stage, int64_t* launches, double* ms);
+/* Kernels of this library launched so far in the process (all contexts). */
+int64_t olc_launch_count(void);
 
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the

@@ -36,11 +36,16 @@ LIB_PATH = os.path.join(HERE, "libolcao_gb300.so")
 
 OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT, OP_HAMILTONIAN = 1, 2, 3, 4, 6
 PREC_FP64, PREC_MIXED = 0, 1
+FORM_FUSED, FORM_STORED = 0, 1
+ITER_EIG_DEVICE, ITER_COEFF_DEVICE = 1, 2
 
 EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_get_dims", "olc_set_stream", "olc_gauss_overlap",
            "olc_ortho_pack", "olc_assemble_hamiltonian", "olc_solve_zhegv",
-           "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch")
+           "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch",
+           "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
+           "olc_launch_count", "olc_scf_matrices")
+STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve")
 
 _LIB: Optional[C.CDLL] = None
 
@@ -76,11 +81,17 @@ def lib() -> C.CDLL:
         L.olc_ortho_pack.argtypes = [vp, i32, dp, dp, dp, dp, dp]
         L.olc_assemble_hamiltonian.argtypes = [vp, dp, dp, i32, dp]
         L.olc_solve_zhegv.argtypes = [vp, dp, dp, i32, dp, dp, dp]
-        L.olc_scf_prepare.argtypes = [vp, i32]
+        L.olc_scf_prepare.argtypes = [vp, i32, i32]
         L.olc_scf_iteration.argtypes = [vp, dp, i32, i32, dp, i32, dp]
         L.olc_primitive_batch.argtypes = [i32, i32, dp, dp, dp]
+        L.olc_profile_enable.argtypes = [vp, i32]
+        L.olc_profile_reset.argtypes = [vp]
+        L.olc_profile_read.argtypes = [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
         for name in EXPORTS[2:]:
             getattr(L, name).restype = C.c_int
+        L.olc_scf_matrices.argtypes = [vp, dp, i32, dp, dp, i32]
+        L.olc_launch_count.restype = C.c_int64
+        L.olc_launch_count.argtypes = []
         _LIB = L
     return _LIB
 
@@ -102,6 +113,11 @@ def _ptr(t) -> Optional[int]:
     if isinstance(t, np.ndarray):
         return t.ctypes.data
     return t.data_ptr()
+
+
+def launch_count() -> int:
+    """Kernels of this library launched so far in the process."""
+    return int(lib().olc_launch_count())
 
 
 def primitive_batch(kind: int, params: np.ndarray, lmalpha: np.ndarray) -> np.ndarray:
@@ -145,6 +161,22 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def profile(self, on: bool = True):
+        _check(lib().olc_profile_enable(self.h, int(on)))
+
+    def profile_reset(self):
+        _check(lib().olc_profile_reset(self.h))
+
+    def profile_read(self) -> Dict[str, Tuple[int, float]]:
+        """{stage: (kernel launches, milliseconds)} since the last reset."""
+        out = {}
+        for i, name in enumerate(STAGES):
+            n = C.c_int64()
+            ms = C.c_double()
+            _check(lib().olc_profile_read(self.h, i, C.byref(n), C.byref(ms)))
+            out[name] = (int(n.value), float(ms.value))
+        return out
 
     def set_stream(self, stream):
         _check(lib().olc_set_stream(self.h, C.c_void_p(stream.cuda_stream)))
@@ -213,17 +245,36 @@ class Context:
                                      num_states, eig.data_ptr(), _ptr(vec), info.ctypes.data))
         return eig, vec, info
 
-    def scf_prepare(self, precision: int = PREC_FP64):
-        _check(lib().olc_scf_prepare(self.h, precision))
+    def scf_prepare(self, precision: int = PREC_FP64, form: int = FORM_FUSED):
+        _check(lib().olc_scf_prepare(self.h, precision, form))
+
+    def scf_matrices(self, coeffs, k: int):
+        """Full Hermitian H(k), S(k) of the prepared pass, as host arrays."""
+        co = np.ascontiguousarray(coeffs, np.float64)
+        n = self.vale_dim
+        H = np.zeros((n, n), np.complex128)
+        Sm = np.zeros((n, n), np.complex128)
+        _check(lib().olc_scf_matrices(self.h, co.ctypes.data, k, H.ctypes.data,
+                                      Sm.ctypes.data, 0))
+        # memory is column-major: transpose to [row, col]
+        return H.T.copy(), Sm.T.copy()
 
     def scf_iteration(self, coeffs, num_states: int, precision: int = PREC_FP64,
                       eig_out=None, vectors=None):
-        """One SCF pass; returns eigenvalues [nk, num_states].  eig_out may be
-        a host numpy array or a device tensor."""
-        co = np.ascontiguousarray(coeffs, np.float64)
+        """One SCF pass; returns eigenvalues [nk, num_states].  coeffs and
+        eig_out may each be host numpy arrays or device tensors."""
+        flags = 0
+        if isinstance(coeffs, np.ndarray) or not hasattr(coeffs, "data_ptr"):
+            co = np.ascontiguousarray(coeffs, np.float64)
+            cptr = co.ctypes.data
+        else:
+            co = coeffs
+            cptr = coeffs.data_ptr()
+            flags |= ITER_COEFF_DEVICE
         if eig_out is None:
             eig_out = np.zeros((self.nk, num_states))
-        on_dev = 0 if isinstance(eig_out, np.ndarray) else 1
-        _check(lib().olc_scf_iteration(self.h, co.ctypes.data, precision, num_states,
-                                       _ptr(eig_out), on_dev, _ptr(vectors)))
+        if not isinstance(eig_out, np.ndarray):
+            flags |= ITER_EIG_DEVICE
+        _check(lib().olc_scf_iteration(self.h, cptr, precision, num_states,
+                                       _ptr(eig_out), flags, _ptr(vectors)))
         return eig_out

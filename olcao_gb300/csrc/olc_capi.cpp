@@ -1,4 +1,5 @@
 // C ABI of libolcao_gb300 (declared in include/olcao_gpu.h).
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -12,6 +13,58 @@ thread_local std::string g_last_error;
 }
 
 void set_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+
+cudaEvent_t take_event(olc_context* ctx) {
+  if (!ctx->prof_pool.empty()) {
+    cudaEvent_t e = ctx->prof_pool.back();
+    ctx->prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void drain_profile(olc_context* ctx) {
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& r : ctx->prof_pending) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->prof_ms[r.stage] += ms;
+    ctx->prof_pool.push_back(r.a);
+    ctx->prof_pool.push_back(r.b);
+  }
+  ctx->prof_pending.clear();
+}
+}  // namespace
+
+void count_launch(int n) { g_launches += n; }
+
+StageScope::StageScope(olc_context* ctx, int stage, int launches)
+    : ctx_(ctx), stage_(stage), launches_(launches) {
+  count_launch(launches);
+  if (ctx_ && ctx_->profiling) {
+    a_ = take_event(ctx_);
+    cudaEventRecord(a_, ctx_->stream);
+  }
+}
+
+void StageScope::add_launches(int n) {
+  launches_ += n;
+  count_launch(n);
+}
+
+StageScope::~StageScope() {
+  if (!ctx_) return;
+  if (ctx_->profiling && a_) {
+    cudaEvent_t b = take_event(ctx_);
+    cudaEventRecord(b, ctx_->stream);
+    ctx_->prof_pending.push_back(StageEvent{stage_, a_, b});
+  }
+  ctx_->prof_launches[stage_] += launches_;
+}
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -79,9 +132,19 @@ int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
 int olc_destroy(olc_context_t* ctx) {
   if (!ctx) return OLC_OK;
   cudaStreamSynchronize(ctx->stream);
+  drain_profile(ctx);
+  for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
   for (void* p : ctx->allocations) cudaFree(p);
-  for (int c = 0; c < kNumClasses; ++c) (void)c;
   if (ctx->d_solver_work) cudaFree(ctx->d_solver_work);
+  for (size_t i = 0; i < ctx->sub_streams.size(); ++i) {
+    cudaStreamSynchronize(ctx->sub_streams[i]);
+    cusolverDnDestroy(ctx->sub_solvers[i]);
+    cudaFree(ctx->sub_work[i]);
+    cudaFree(ctx->sub_eval[i]);
+    cudaStreamDestroy(ctx->sub_streams[i]);
+    cudaEventDestroy(ctx->ev_join[i]);
+  }
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->blas) cublasDestroy(ctx->blas);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
   delete ctx;
@@ -153,16 +216,49 @@ int olc_solve_zhegv(olc_context_t* ctx, const double* packed_h, const double* pa
   return solve_packed(ctx, packed_h, packed_s, num_states, eigenvalues, vectors, info);
 }
 
-int olc_scf_prepare(olc_context_t* ctx, int precision) {
+int olc_scf_prepare(olc_context_t* ctx, int precision, int form) {
   if (!ctx) return fail(OLC_ERR_ARG, "olc_scf_prepare: null context");
-  return scf_prepare(ctx, precision);
+  if (form != OLC_FORM_FUSED && form != OLC_FORM_STORED) return fail(OLC_ERR_ARG, "olc_scf_prepare: bad form");
+  return scf_prepare(ctx, precision, form);
 }
 
 int olc_scf_iteration(olc_context_t* ctx, const double* coeffs, int precision, int num_states,
-                      double* eigenvalues, int eig_on_device, double* vectors) {
+                      double* eigenvalues, int flags, double* vectors) {
   if (!ctx || !coeffs || !eigenvalues) return fail(OLC_ERR_ARG, "olc_scf_iteration: null argument");
-  return scf_iteration(ctx, coeffs, precision, num_states, eigenvalues, eig_on_device, vectors);
+  return scf_iteration(ctx, coeffs, precision, num_states, eigenvalues, flags, vectors);
 }
+
+int olc_scf_matrices(olc_context_t* ctx, const double* coeffs, int kpoint, double* h, double* s,
+                     int on_device) {
+  if (!ctx || !coeffs) return fail(OLC_ERR_ARG, "olc_scf_matrices: null argument");
+  return scf_matrices(ctx, coeffs, kpoint, h, s, on_device);
+}
+
+int olc_profile_enable(olc_context_t* ctx, int on) {
+  if (!ctx) return fail(OLC_ERR_ARG, "olc_profile_enable: null context");
+  ctx->profiling = on != 0;
+  return OLC_OK;
+}
+
+int olc_profile_reset(olc_context_t* ctx) {
+  if (!ctx) return fail(OLC_ERR_ARG, "olc_profile_reset: null context");
+  drain_profile(ctx);
+  for (int s = 0; s < OLC_NUM_STAGES; ++s) {
+    ctx->prof_ms[s] = 0.0;
+    ctx->prof_launches[s] = 0;
+  }
+  return OLC_OK;
+}
+
+int olc_profile_read(olc_context_t* ctx, int stage, int64_t* launches, double* ms) {
+  if (!ctx || stage < 0 || stage >= OLC_NUM_STAGES) return fail(OLC_ERR_ARG, "olc_profile_read: bad argument");
+  drain_profile(ctx);
+  if (launches) *launches = ctx->prof_launches[stage];
+  if (ms) *ms = ctx->prof_ms[stage];
+  return OLC_OK;
+}
+
+int64_t olc_launch_count(void) { return g_launches.load(); }
 
 int olc_primitive_batch(int kind, int n, const double* in, const int32_t* lmalpha, double* out) {
   if (n > 0 && (!in || !lmalpha || !out)) return fail(OLC_ERR_ARG, "olc_primitive_batch: null argument");

@@ -96,6 +96,12 @@ struct ItemLists {
   int64_t total_sh;                     // doubles of sh scratch
 };
 
+// Per-stage CUDA-event timing on the context stream.
+struct StageEvent {
+  int stage;
+  cudaEvent_t a, b;
+};
+
 }  // namespace olc
 
 struct olc_context {
@@ -122,6 +128,8 @@ struct olc_context {
   // cached iteration-invariant data (olc_scf_prepare)
   bool prepared = false;
   int prep_precision = 0;
+  int prep_form = 0;
+  double* d_terms = nullptr;       // stored form: packed NP, KE, V_j [2+pd][nk][plen][2]
   double* d_scv = nullptr;         // S core-vale  [nk][nv][nc] complex
   double* d_h0 = nullptr;          // ortho(KE + NP) full upper [nk][nv][nv] complex
   double* d_chol = nullptr;        // Cholesky factor of ortho'd S, [nk][nv][nv]
@@ -133,13 +141,43 @@ struct olc_context {
   double* d_work_w = nullptr;
   void* d_solver_work = nullptr;
   size_t solver_work_bytes = 0;
+  // independent k-point solves run concurrently on sub-streams
+  std::vector<cudaStream_t> sub_streams;
+  std::vector<cusolverDnHandle_t> sub_solvers;
+  std::vector<void*> sub_work;
+  std::vector<double*> sub_eval;
+  size_t sub_work_bytes = 0;
+  int sub_n = 0;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_join;
   int* d_info = nullptr;
   double* d_eval = nullptr;
+  // profiling
+  bool profiling = false;
+  std::vector<olc::StageEvent> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+  double prof_ms[OLC_NUM_STAGES] = {};
+  int64_t prof_launches[OLC_NUM_STAGES] = {};
 };
 
 namespace olc {
 
 void set_error(const std::string& msg);
+void count_launch(int n = 1);
+
+// Records a stage's start on construction and its end on destruction when the
+// context is profiling; `launches` kernels are attributed to the stage.
+class StageScope {
+ public:
+  StageScope(olc_context* ctx, int stage, int launches = 1);
+  ~StageScope();
+  void add_launches(int n);
+ private:
+  olc_context* ctx_;
+  int stage_;
+  int launches_;
+  cudaEvent_t a_ = nullptr;
+};
 int fail(int code, const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
 
@@ -172,8 +210,10 @@ int assemble_packed(olc_context* ctx, const double* const* terms, const double* 
                     int nterm, double* out);
 int solve_packed(olc_context* ctx, const double* packed_h, const double* packed_s,
                  int num_states, double* eigenvalues, double* vectors, int32_t* info);
-int scf_prepare(olc_context* ctx, int precision);
+int scf_prepare(olc_context* ctx, int precision, int form);
+int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, double* s,
+                 int on_device);
 int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
-                  double* eigenvalues, int eig_on_device, double* vectors);
+                  double* eigenvalues, int flags, double* vectors);
 
 }  // namespace olc

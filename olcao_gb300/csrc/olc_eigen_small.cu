@@ -10,7 +10,9 @@
 //                                      parallel (round-robin) pair ordering
 //   4. X = U^{-1} V                   (back-transform, X^H S X = I)
 // Eigenvalues are returned in ascending order with their vectors.
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 
 #include "olc_common.h"
 
@@ -29,7 +31,7 @@ __device__ __forceinline__ cd csub(cd a, cd b) { return {a.x - b.x, a.y - b.y}; 
 __global__ void __launch_bounds__(kThreads) small_hegv_kernel(
     const double* __restrict__ hin, const double* __restrict__ sin_, int n, int num_states,
     int s_factored, double* __restrict__ eig_out, double* __restrict__ vec_out,
-    int32_t* __restrict__ info_out) {
+    int32_t* __restrict__ info_out, double* __restrict__ trace_out) {
   extern __shared__ double smem[];
   const int k = blockIdx.x;
   const int tid = threadIdx.x;
@@ -118,6 +120,10 @@ __global__ void __launch_bounds__(kThreads) small_hegv_kernel(
     }
     __syncthreads();
   }
+  if (trace_out) {
+    double* d0 = trace_out + (size_t)gridDim.x * 82 + (size_t)k * 6 * nn;
+    for (size_t e = tid; e < nn; e += blockDim.x) { d0[2 * e] = C[e].x; d0[2 * e + 1] = C[e].y; }
+  }
   // V = I
   for (size_t e = tid; e < nn; e += blockDim.x) {
     const int r = (int)(e % n), c = (int)(e / n);
@@ -156,7 +162,11 @@ __global__ void __launch_bounds__(kThreads) small_hegv_kernel(
       s_diag = t;
     }
     __syncthreads();
-    if (s_off <= 1e-30 * s_diag || s_off == 0.0) break;
+    if (trace_out && tid == 0 && sweep < 40) {
+      trace_out[(size_t)k * 82 + 2 * sweep] = s_off;
+      trace_out[(size_t)k * 82 + 2 * sweep + 1] = s_diag;
+    }
+    if (s_off <= 1e-28 * s_diag || s_off == 0.0) break;
     for (int round = 0; round < m - 1; ++round) {
       // rotation parameters of this round's disjoint pairs, from the
       // pre-round matrix: J = D R with D = diag(1, e^{-i phi}), R real
@@ -169,9 +179,12 @@ __global__ void __launch_bounds__(kThreads) small_hegv_kernel(
         double c = 1.0, s = 0.0, phx = 1.0, phy = 0.0;
         if (q < n) {
           const cd cpq = C[(size_t)q * n + p];
-          const double b = sqrt(cpq.x * cpq.x + cpq.y * cpq.y);
-          if (b > 1e-300) {
-            const double app = C[(size_t)p * n + p].x, aqq = C[(size_t)q * n + q].x;
+          // hypot keeps |e^{-i phi}| = 1 when the entry is tiny (x*x + y*y
+          // would drop into denormals and make the rotation non-unitary);
+          // entries below 1e-18 of the diagonal scale are left alone
+          const double b = hypot(cpq.x, cpq.y);
+          const double app = C[(size_t)p * n + p].x, aqq = C[(size_t)q * n + q].x;
+          if (b > 1e-300 && b > 1e-18 * (fabs(app) + fabs(aqq))) {
             const double th = (aqq - app) / (2.0 * b);
             const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
             c = 1.0 / sqrt(t * t + 1.0);
@@ -218,6 +231,14 @@ __global__ void __launch_bounds__(kThreads) small_hegv_kernel(
       __syncthreads();
     }
   }
+  if (trace_out) {
+    double* d1 = trace_out + (size_t)gridDim.x * 82 + (size_t)k * 6 * nn + 2 * nn;
+    for (size_t e = tid; e < nn; e += blockDim.x) {
+      d1[2 * e] = C[e].x; d1[2 * e + 1] = C[e].y;
+      d1[2 * nn + 2 * e] = V[e].x; d1[2 * nn + 2 * e + 1] = V[e].y;
+    }
+  }
+  __syncthreads();
   // ---- 4. eigenvalues, sort, back-transform X = U^{-1} V ------------------
   for (int i = tid; i < n; i += blockDim.x) {
     w[i] = C[(size_t)i * n + i].x;
@@ -253,7 +274,17 @@ __global__ void __launch_bounds__(kThreads) small_hegv_kernel(
 
 }  // namespace
 
-int small_solver_max_n() { return kSmallMaxN; }
+// Largest n sent to the batched in-shared-memory solver.  OLC_SMALL_SOLVER_MAX_N
+// lowers it (0 routes every size to the library path; used to cross-check the
+// two solvers on the same matrices).
+int small_solver_max_n() {
+  static int v = -1;
+  if (v < 0) {
+    v = kSmallMaxN;
+    if (const char* e = std::getenv("OLC_SMALL_SOLVER_MAX_N")) v = std::min(kSmallMaxN, std::atoi(e));
+  }
+  return v;
+}
 
 int solve_small_batched(olc_context* ctx, const double* h_full, const double* s_full, int n,
                         int num_states, double* eigenvalues, double* vectors, int32_t* info_host,
@@ -266,9 +297,33 @@ int solve_small_batched(olc_context* ctx, const double* h_full, const double* s_
                        "smem attribute"))) return st;
   int32_t* dinfo = nullptr;
   if ((st = cuda_check(cudaMallocAsync((void**)&dinfo, sizeof(int32_t) * nk, ctx->stream), "malloc info"))) return st;
+  StageScope scope(ctx, OLC_STAGE_SOLVE);
+  // OLC_SMALL_SOLVER_TRACE=1 prints each k-point's Jacobi convergence history
+  double* dtrace = nullptr;
+  static const bool trace = std::getenv("OLC_SMALL_SOLVER_TRACE") != nullptr;
+  if (trace) {
+    const size_t tl = 82 * (size_t)nk + 6 * (size_t)n * n * nk;
+    cudaMalloc(&dtrace, sizeof(double) * tl);
+    cudaMemset(dtrace, 0, sizeof(double) * tl);
+  }
   small_hegv_kernel<<<nk, kThreads, smem, ctx->stream>>>(h_full, s_full, n, num_states,
                                                          s_is_factored ? 1 : 0, eigenvalues,
-                                                         vectors, dinfo);
+                                                         vectors, dinfo, dtrace);
+  if (dtrace) {
+    std::vector<double> ht(82 * (size_t)nk + 6 * (size_t)n * n * nk);
+    cudaMemcpy(ht.data(), dtrace, sizeof(double) * ht.size(), cudaMemcpyDeviceToHost);
+    if (const char* f = std::getenv("OLC_SMALL_SOLVER_TRACE_FILE")) {
+      FILE* fp = std::fopen(f, "wb");
+      if (fp) { std::fwrite(ht.data() + 82 * (size_t)nk, sizeof(double), 6 * (size_t)n * n * nk, fp); std::fclose(fp); }
+    }
+    for (int k = 0; k < nk; ++k) {
+      std::fprintf(stderr, "k=%d", k);
+      for (int q = 0; q < 40 && ht[82 * k + 2 * q + 1] != 0.0; ++q)
+        std::fprintf(stderr, " %.2e", ht[82 * k + 2 * q] / ht[82 * k + 2 * q + 1]);
+      std::fprintf(stderr, "\n");
+    }
+    cudaFree(dtrace);
+  }
   st = cuda_check(cudaGetLastError(), "small_hegv_kernel");
   std::vector<int32_t> hinfo(nk, 0);
   cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(int32_t) * nk, cudaMemcpyDeviceToHost, ctx->stream);

@@ -196,6 +196,7 @@ int launch_class(olc_context* ctx, int cls, const double* coeffs, int ep_type, i
   a.ep_alpha = ep_alpha;
   if (a.n == 0) return OLC_OK;
   const dim3 block(128), grid((a.n + 127) / 128);
+  StageScope scope(ctx, OLC_STAGE_PRIMITIVES);
   switch (cls) {
 #define OLC_CASE(c, l1, l2) \
   case c: prim_kernel<OP, l1, l2><<<grid, block, 0, ctx->stream>>>(ctx->view, a); break;
@@ -388,17 +389,22 @@ int run_contract_bloch(olc_context* ctx, double* vv, double* cv, double* cc) {
   ca.ntasks = ntasks;
   ca.ms = ctx->max_states;
   ca.block = ctx->d_block;
-  contract_kernel<<<(ntasks + 7) / 8, 256, 0, ctx->stream>>>(v, ca);
+  {
+    StageScope scope(ctx, OLC_STAGE_CONTRACT);
+    contract_kernel<<<(ntasks + 7) / 8, 256, 0, ctx->stream>>>(v, ca);
+  }
   if ((st = cuda_check(cudaGetLastError(), "contract_kernel"))) return st;
   BlochArgs ba;
+  const int per_k_cap = 256;
   ba.block = ctx->d_block;
   ba.ms = ctx->max_states;
   const int per_k = ctx->max_states * ctx->max_states;
-  ba.kchunk = std::max(1, std::min((int)nk, 2048 / std::max(1, per_k)));
+  ba.kchunk = std::max(1, std::min((int)nk, per_k_cap * 4 / std::max(1, per_k)));
   ba.vv = vv;
   ba.cv = cv;
   ba.cc = cc;
   dim3 grid((unsigned)ctx->hpairs.size(), (unsigned)((nk + ba.kchunk - 1) / ba.kchunk));
+  StageScope scope(ctx, OLC_STAGE_BLOCH);
   bloch_scatter_kernel<<<grid, 256, 0, ctx->stream>>>(v, ba);
   return cuda_check(cudaGetLastError(), "bloch_scatter_kernel");
 }
@@ -406,6 +412,7 @@ int run_contract_bloch(olc_context* ctx, double* vv, double* cv, double* cc) {
 int build_phase_table(olc_context* ctx) {
   const SysView& v = ctx->view;
   const int n = v.nk * v.ncells;
+  count_launch();
   phase_table_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(v, const_cast<double*>(v.phase));
   return cuda_check(cudaGetLastError(), "phase_table_kernel");
 }
@@ -477,6 +484,7 @@ int primitive_batch_device(int kind, int n, const double* in, const int32_t* lma
   if (!st) st = cuda_check(cudaMemcpy(dlm, lmalpha, sizeof(int32_t) * 2 * n, cudaMemcpyHostToDevice), "copy");
   if (!st) st = cuda_check(cudaMemset(dout, 0, sizeof(double) * 256 * n), "memset");
   if (!st) {
+    count_launch();
     prim_batch_kernel<<<(n + 63) / 64, 64>>>(kind, n, din, dlm, dout);
     st = cuda_check(cudaGetLastError(), "prim_batch_kernel");
   }

@@ -138,6 +138,14 @@ __global__ void assemble_kernel(const double* const* terms, const double* coeffs
   }
 }
 
+// multipliers: leading `off` terms (NP, KE) weigh 1; an exact 0 counts as 1
+__global__ void fix_coeff_kernel(double* c, int n, int off) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (i < off) c[i] = 1.0;
+    else if (c[i] == 0.0) c[i] = 1.0;
+  }
+}
+
 __global__ void gather_eigs_kernel(const double* w, int n, int nstates, int k, double* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nstates) out[(size_t)k * nstates + i] = w[i];
@@ -157,6 +165,7 @@ int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const dou
                   const double* add) {
   const int nv = ctx->dims.vale_dim, nc = ctx->dims.core_dim, nk = ctx->dims.num_kpoints;
   int st;
+  StageScope scope(ctx, OLC_STAGE_ORTHO);
   if (nc) {
     const size_t nn = (size_t)nv * nv;
     if (!ctx->d_work_x) {
@@ -221,7 +230,10 @@ int assemble_packed(olc_context* ctx, const double* const* terms, const double* 
   if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * nterm, ctx->stream), "malloc"))) return st;
   cudaMemcpyAsync(dterms, terms, sizeof(double*) * nterm, cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(dco, coeffs, sizeof(double) * nterm, cudaMemcpyHostToDevice, ctx->stream);
-  assemble_kernel<<<grid_for(len), 256, 0, ctx->stream>>>(dterms, dco, nterm, len, out);
+  {
+    StageScope scope(ctx, OLC_STAGE_ASSEMBLE);
+    assemble_kernel<<<grid_for(len), 256, 0, ctx->stream>>>(dterms, dco, nterm, len, out);
+  }
   st = cuda_check(cudaGetLastError(), "assemble_kernel");
   cudaFreeAsync(dterms, ctx->stream);
   cudaFreeAsync(dco, ctx->stream);
@@ -230,30 +242,59 @@ int assemble_packed(olc_context* ctx, const double* const* terms, const double* 
 }
 
 // Generalised eigen-problem per k on full Hermitian matrices h, s (both
-// overwritten).  Library path: cuSOLVER zhegvd (same algorithm as LAPACK
-// zhegv: Cholesky, reduction, tridiagonal solve, back-transform).
+// overwritten).  Library path: cuSOLVER zhegvd (the algorithm of LAPACK
+// zhegv: Cholesky, reduction, tridiagonal solve, back-transform).  The k-points
+// are independent problems, so they are spread over concurrent sub-streams,
+// each with its own solver handle and workspace.
 int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
                        double* eigenvalues, int eig_on_device, double* vectors, int32_t* info) {
   const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   const size_t nn = (size_t)n * n;
   int st;
-  if (!ctx->d_eval) {
-    if ((st = dalloc(ctx, &ctx->d_eval, (size_t)n))) return st;
-    if ((st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
+  const int nsub = std::max(1, std::min(nk, 16));
+  if ((int)ctx->sub_streams.size() != nsub || ctx->sub_n != n) {
+    for (size_t i = 0; i < ctx->sub_streams.size(); ++i) {
+      cudaStreamSynchronize(ctx->sub_streams[i]);
+      cusolverDnDestroy(ctx->sub_solvers[i]);
+      cudaFree(ctx->sub_work[i]);
+      cudaFree(ctx->sub_eval[i]);
+      cudaStreamDestroy(ctx->sub_streams[i]);
+      cudaEventDestroy(ctx->ev_join[i]);
+    }
+    ctx->sub_streams.clear(); ctx->sub_solvers.clear(); ctx->sub_work.clear();
+    ctx->sub_eval.clear(); ctx->ev_join.clear();
+    if (!ctx->ev_fork) cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    int lwork = 0;
+    cusolverDnHandle_t h0;
+    if (cusolverDnCreate(&h0) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
+    cusolverStatus_t ss = cusolverDnZhegvd_bufferSize(
+        h0, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+        reinterpret_cast<cuDoubleComplex*>(h), n, reinterpret_cast<cuDoubleComplex*>(s), n,
+        nullptr, &lwork);
+    cusolverDnDestroy(h0);
+    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "zhegvd_bufferSize failed");
+    ctx->sub_work_bytes = sizeof(cuDoubleComplex) * (size_t)lwork;
+    for (int i = 0; i < nsub; ++i) {
+      cudaStream_t sm;
+      cusolverDnHandle_t hs;
+      void* w = nullptr;
+      double* ev = nullptr;
+      cudaEvent_t ej;
+      if ((st = cuda_check(cudaStreamCreateWithFlags(&sm, cudaStreamNonBlocking), "sub stream"))) return st;
+      if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
+      cusolverDnSetStream(hs, sm);
+      if ((st = cuda_check(cudaMalloc(&w, ctx->sub_work_bytes), "solver work"))) return st;
+      if ((st = cuda_check(cudaMalloc((void**)&ev, sizeof(double) * n), "solver eval"))) return st;
+      cudaEventCreateWithFlags(&ej, cudaEventDisableTiming);
+      ctx->sub_streams.push_back(sm);
+      ctx->sub_solvers.push_back(hs);
+      ctx->sub_work.push_back(w);
+      ctx->sub_eval.push_back(ev);
+      ctx->ev_join.push_back(ej);
+    }
+    ctx->sub_n = n;
   }
-  int lwork = 0;
-  cusolverStatus_t ss = cusolverDnZhegvd_bufferSize(
-      ctx->solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
-      reinterpret_cast<cuDoubleComplex*>(h), n, reinterpret_cast<cuDoubleComplex*>(s), n,
-      ctx->d_eval, &lwork);
-  if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "zhegvd_bufferSize failed");
-  const size_t need = sizeof(cuDoubleComplex) * (size_t)lwork;
-  if (need > ctx->solver_work_bytes) {
-    if (ctx->d_solver_work) cudaFree(ctx->d_solver_work);
-    ctx->d_solver_work = nullptr;
-    if ((st = cuda_check(cudaMalloc(&ctx->d_solver_work, need), "solver work"))) return st;
-    ctx->solver_work_bytes = need;
-  }
+  if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
   double* eig_dev = eigenvalues;
   double* tmp_eigs = nullptr;
   if (!eig_on_device) {
@@ -261,20 +302,31 @@ int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
                                          ctx->stream), "malloc eigs"))) return st;
     eig_dev = tmp_eigs;
   }
+  const int lwork = (int)(ctx->sub_work_bytes / sizeof(cuDoubleComplex));
+  StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
+  cudaEventRecord(ctx->ev_fork, ctx->stream);
+  for (int i = 0; i < nsub; ++i) cudaStreamWaitEvent(ctx->sub_streams[i], ctx->ev_fork, 0);
   for (int k = 0; k < nk; ++k) {
+    const int i = k % nsub;
+    cudaStream_t sm = ctx->sub_streams[i];
     auto* H = reinterpret_cast<cuDoubleComplex*>(h) + (size_t)k * nn;
     auto* S = reinterpret_cast<cuDoubleComplex*>(s) + (size_t)k * nn;
-    ss = cusolverDnZhegvd(ctx->solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-                          CUBLAS_FILL_MODE_UPPER, n, H, n, S, n, ctx->d_eval,
-                          reinterpret_cast<cuDoubleComplex*>(ctx->d_solver_work), lwork,
-                          ctx->d_info + k);
+    cusolverStatus_t ss = cusolverDnZhegvd(ctx->sub_solvers[i], CUSOLVER_EIG_TYPE_1,
+                                           CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, H,
+                                           n, S, n, ctx->sub_eval[i],
+                                           reinterpret_cast<cuDoubleComplex*>(ctx->sub_work[i]),
+                                           lwork, ctx->d_info + k);
     if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnZhegvd failed");
-    gather_eigs_kernel<<<(num_states + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_eval, n,
-                                                                          num_states, k, eig_dev);
+    scope.add_launches(1);
+    gather_eigs_kernel<<<(num_states + 127) / 128, 128, 0, sm>>>(ctx->sub_eval[i], n, num_states,
+                                                                 k, eig_dev);
     if (vectors)
       cudaMemcpyAsync(vectors + 2 * (size_t)k * n * num_states, H,
-                      sizeof(cuDoubleComplex) * (size_t)n * num_states, cudaMemcpyDeviceToDevice,
-                      ctx->stream);
+                      sizeof(cuDoubleComplex) * (size_t)n * num_states, cudaMemcpyDeviceToDevice, sm);
+  }
+  for (int i = 0; i < nsub; ++i) {
+    cudaEventRecord(ctx->ev_join[i], ctx->sub_streams[i]);
+    cudaStreamWaitEvent(ctx->stream, ctx->ev_join[i], 0);
   }
   if (!eig_on_device) {
     cudaMemcpyAsync(eigenvalues, tmp_eigs, sizeof(double) * (size_t)num_states * nk,
@@ -329,8 +381,11 @@ int solve_packed(olc_context* ctx, const double* packed_h, const double* packed_
   int st;
   if ((st = cuda_check(cudaMalloc(&h, 16 * nn * nk), "malloc h"))) return st;
   if ((st = cuda_check(cudaMalloc(&s, 16 * nn * nk), "malloc s"))) { cudaFree(h); return st; }
-  unpack_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(packed_h, h, n, nk);
-  unpack_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(packed_s, s, n, nk);
+  {
+    StageScope scope(ctx, OLC_STAGE_ASSEMBLE, 2);
+    unpack_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(packed_h, h, n, nk);
+    unpack_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(packed_s, s, n, nk);
+  }
   st = cuda_check(cudaGetLastError(), "unpack_kernel");
   if (!st) st = solve_full(ctx, h, s, num_states, eigenvalues, 1, vectors, info);
   cudaStreamSynchronize(ctx->stream);
@@ -342,9 +397,49 @@ int solve_packed(olc_context* ctx, const double* packed_h, const double* packed_
 // ---------------------------------------------------------------------------
 // SCF pass
 // ---------------------------------------------------------------------------
-int scf_prepare(olc_context* ctx, int precision) {
+namespace {
+
+// Stored form: H(k) = NP + KE + sum_j c_j V_j from the resident packed terms,
+// written straight into the full Hermitian matrix the solver consumes (the
+// packed read, readPackedMatrixAccum and unpackMatrix in one pass).
+__global__ void assemble_full_kernel(const double* __restrict__ terms, const double* __restrict__ c,
+                                     int nterm, int n, int nk, double* __restrict__ full) {
+  const size_t plen = (size_t)n * (n + 1) / 2;
+  const size_t total = plen * nk;
+  const size_t tstride = 2 * plen * nk;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / plen);
+    const size_t r = idx % plen;
+    int i = (int)((sqrt(8.0 * (double)r + 1.0) - 1.0) * 0.5);
+    while ((size_t)i * (i + 1) / 2 > r) --i;
+    while ((size_t)(i + 1) * (i + 2) / 2 <= r) ++i;
+    const int j = (int)(r - (size_t)i * (i + 1) / 2);
+    const double2* t2 = reinterpret_cast<const double2*>(terms);
+    double2 acc = t2[idx];
+    for (int t = 1; t < nterm; ++t) {
+      const double2 x = t2[(size_t)t * (tstride / 2) + idx];
+      const double w = c[t];
+      acc.x += w * x.x;
+      acc.y += w * x.y;
+    }
+    double2* f = reinterpret_cast<double2*>(full) + (size_t)k * n * n;
+    if (i == j) {
+      f[(size_t)i * n + i] = make_double2(acc.x, 0.0);
+    } else {
+      f[(size_t)i * n + j] = acc;                               // (row j, col i)
+      f[(size_t)j * n + i] = make_double2(acc.x, -acc.y);       // (row i, col j)
+    }
+  }
+}
+
+}  // namespace
+
+int scf_prepare(olc_context* ctx, int precision, int form) {
   const int nv = ctx->dims.vale_dim, nc = ctx->dims.core_dim, nk = ctx->dims.num_kpoints;
+  const int pd = ctx->dims.pot_dim;
   const size_t nn = (size_t)nv * nv;
+  const size_t plen2 = 2 * (size_t)ctx->dims.packed_len * nk;   // doubles per packed term
   int st;
   if (!ctx->d_work_vv) {
     if ((st = dalloc(ctx, &ctx->d_work_vv, 2 * nn * nk))) return st;
@@ -353,7 +448,6 @@ int scf_prepare(olc_context* ctx, int precision) {
       if ((st = dalloc(ctx, &ctx->d_work_cc, 2 * (size_t)nc * nc * nk))) return st;
       if ((st = dalloc(ctx, &ctx->d_scv, 2 * (size_t)nc * nv * nk))) return st;
     }
-    if ((st = dalloc(ctx, &ctx->d_h0, 2 * nn * nk))) return st;
     if ((st = dalloc(ctx, &ctx->d_chol, 2 * nn * nk))) return st;   // orthogonalised S
   }
   // S: overlap integrals, keep S_cv, orthogonalise
@@ -361,50 +455,109 @@ int scf_prepare(olc_context* ctx, int precision) {
   if ((st = run_contract_bloch(ctx, ctx->d_work_vv, nc ? ctx->d_scv : nullptr, ctx->d_work_cc))) return st;
   if ((st = ortho_pack_ex(ctx, true, ctx->d_work_vv, ctx->d_scv, ctx->d_work_cc, ctx->d_scv,
                           nullptr, ctx->d_chol, nullptr))) return st;
-  // H0 = KE + NP in one pass
-  if ((st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, OLC_PREC_FP64, false))) return st;
-  if ((st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, OLC_PREC_FP64, true))) return st;
-  if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
-  if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
-                          nullptr, ctx->d_h0, nullptr))) return st;
+  count_launch();
+  hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(ctx->d_chol, nv, nk);
+  if (form == OLC_FORM_STORED) {
+    if (!ctx->d_terms && (st = dalloc(ctx, &ctx->d_terms, plen2 * (2 + pd)))) return st;
+    // term 0 = NP, 1 = KE, 2 + j = V_j (the order the reference sums them)
+    const int ops[2] = {OLC_OP_NUCLEAR, OLC_OP_KINETIC};
+    for (int t = 0; t < 2 + pd; ++t) {
+      const int op = t < 2 ? ops[t] : OLC_OP_ELECPOT;
+      if ((st = run_primitives(ctx, op, t < 2 ? 0 : t - 2, nullptr, OLC_PREC_FP64, false))) return st;
+      if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
+      if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc,
+                              ctx->d_scv, ctx->d_terms + (size_t)t * plen2, nullptr, nullptr))) return st;
+    }
+  } else {
+    if (!ctx->d_h0 && (st = dalloc(ctx, &ctx->d_h0, 2 * nn * nk))) return st;
+    // H0 = KE + NP in one pass
+    if ((st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, OLC_PREC_FP64, false))) return st;
+    if ((st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, OLC_PREC_FP64, true))) return st;
+    if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
+    if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
+                            nullptr, ctx->d_h0, nullptr))) return st;
+  }
   ctx->prepared = true;
   ctx->prep_precision = precision;
+  ctx->prep_form = form;
   return cuda_check(cudaStreamSynchronize(ctx->stream), "prepare sync");
 }
 
+// Builds H(k) (full Hermitian, all k) for the prepared form into h.
+int build_hamiltonian(olc_context* ctx, const double* coeffs, int precision, int flags, double* h);
+
+int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, double* s,
+                 int on_device) {
+  if (!ctx->prepared) return fail(OLC_ERR_ARG, "olc_scf_matrices before olc_scf_prepare");
+  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
+  if (kpoint < 0 || kpoint >= nk) return fail(OLC_ERR_ARG, "k-point out of range");
+  const size_t nn = (size_t)nv * nv;
+  double* hall = nullptr;
+  int st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&hall, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
+  st = build_hamiltonian(ctx, coeffs, ctx->prep_precision, 0, hall);
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (!st && h) st = cuda_check(cudaMemcpyAsync(h, hall + 2 * nn * kpoint, 16 * nn, kind, ctx->stream), "copy h");
+  if (!st && s) st = cuda_check(cudaMemcpyAsync(s, ctx->d_chol + 2 * nn * kpoint, 16 * nn, kind, ctx->stream), "copy s");
+  cudaFreeAsync(hall, ctx->stream);
+  int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "matrices sync");
+  return st ? st : s2;
+}
+
 int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
-                  double* eigenvalues, int eig_on_device, double* vectors) {
+                  double* eigenvalues, int flags, double* vectors) {
   if (!ctx->prepared) return fail(OLC_ERR_ARG, "olc_scf_iteration before olc_scf_prepare");
-  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints, pd = ctx->dims.pot_dim;
+  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   if (num_states < 1 || num_states > nv) return fail(OLC_ERR_ARG, "num_states out of range");
   const size_t nn = (size_t)nv * nv;
   int st;
-  // the reference adds a term with multiplier 0 unscaled (matrixSubs.F90:278-282)
-  std::vector<double> c(coeffs, coeffs + pd);
-  for (auto& x : c)
-    if (x == 0.0) x = 1.0;
-  double* dco = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * std::max(1, pd), ctx->stream), "malloc coeffs"))) return st;
-  cudaMemcpyAsync(dco, c.data(), sizeof(double) * pd, cudaMemcpyHostToDevice, ctx->stream);
-  st = run_primitives(ctx, OLC_OP_ELECPOT, 0, dco, precision, false);
-  cudaFreeAsync(dco, ctx->stream);
-  if (st) return st;
-  if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
-  // H' = ortho(V) + H0 written into the work matrix (upper), S' copied
   double *h = nullptr, *s = nullptr;
   if ((st = cuda_check(cudaMallocAsync((void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
-  if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
-                          nullptr, h, ctx->d_h0))) return st;
+  if ((st = build_hamiltonian(ctx, coeffs, precision, flags, h))) return st;
   cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
-  hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(h, nv, nk);
-  hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(s, nv, nk);
-  if ((st = cuda_check(cudaGetLastError(), "hermitize"))) return st;
-  st = solve_full(ctx, h, s, num_states, eigenvalues, eig_on_device, vectors, nullptr);
+  st = solve_full(ctx, h, s, num_states, eigenvalues, (flags & OLC_ITER_EIG_DEVICE) ? 1 : 0,
+                  vectors, nullptr);
   cudaFreeAsync(h, ctx->stream);
   cudaFreeAsync(s, ctx->stream);
   int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "iteration sync");
   return st ? st : s2;
+}
+
+int build_hamiltonian(olc_context* ctx, const double* coeffs, int precision, int flags, double* h) {
+  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints, pd = ctx->dims.pot_dim;
+  const size_t nn = (size_t)nv * nv;
+  int st;
+  // coefficients on the device; the reference adds a term whose multiplier
+  // is exactly 0 unscaled (matrixSubs.F90:278-282)
+  double* dco = nullptr;
+  const int off = ctx->prep_form == OLC_FORM_STORED ? 2 : 0;
+  if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * (pd + 2), ctx->stream), "malloc coeffs"))) return st;
+  if (flags & OLC_ITER_COEFF_DEVICE) {
+    cudaMemcpyAsync(dco + off, coeffs, sizeof(double) * pd, cudaMemcpyDeviceToDevice, ctx->stream);
+  } else {
+    cudaMemcpyAsync(dco + off, coeffs, sizeof(double) * pd, cudaMemcpyHostToDevice, ctx->stream);
+  }
+  count_launch();
+  fix_coeff_kernel<<<1, 64, 0, ctx->stream>>>(dco, pd + off, off);
+  if (ctx->prep_form == OLC_FORM_STORED) {
+    const size_t plen = (size_t)ctx->dims.packed_len;
+    StageScope scope(ctx, OLC_STAGE_ASSEMBLE);
+    assemble_full_kernel<<<grid_for(plen * nk), 256, 0, ctx->stream>>>(ctx->d_terms, dco, pd + 2,
+                                                                        nv, nk, h);
+    if ((st = cuda_check(cudaGetLastError(), "assemble_full_kernel"))) return st;
+  } else {
+    st = run_primitives(ctx, OLC_OP_ELECPOT, 0, dco, precision, false);
+    if (st) { cudaFreeAsync(dco, ctx->stream); return st; }
+    if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
+    // H' = ortho(V) + H0, upper, then mirrored
+    if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
+                            nullptr, h, ctx->d_h0))) return st;
+    StageScope scope(ctx, OLC_STAGE_ASSEMBLE);
+    hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(h, nv, nk);
+  }
+  cudaFreeAsync(dco, ctx->stream);
+  return cuda_check(cudaGetLastError(), "hamiltonian kernels");
 }
 
 }  // namespace olc

@@ -643,14 +643,24 @@ struct Oracle {
     if (cv) std::fill(cv, cv + nc * nv * nk, cplx(0, 0));
     if (cc) std::fill(cc, cc + nc * nc * nk, cplx(0, 0));
     const int MS = OLC_MAX_STATES;
+    std::vector<std::pair<int, int>> pairList;
+    for (int i = 0; i < nsites; ++i)
+      for (int j = i; j < nsites; ++j) pairList.push_back({i, j});
+    int status = OLC_OK;
+    // atom pairs are independent and scatter into disjoint blocks
+#pragma omp parallel
+    {
     std::vector<cplx> cur((size_t)MS * MS * nk);
     std::vector<double> pairX(16 * OLC_MAX_ALPHAS * MS);
-    double block[OLC_MAX_STATES * OLC_MAX_STATES];
+    std::vector<double> blockv(OLC_MAX_STATES * OLC_MAX_STATES);
+    double* block = blockv.data();
     double sh[256];
-    for (int i = 0; i < nsites; ++i) {
+#pragma omp for schedule(dynamic, 1)
+    for (long pi = 0; pi < (long)pairList.size(); ++pi) {
+      const int i = pairList[pi].first, j = pairList[pi].second;
       const TypeInfo& t1 = types[siteType[i]];
       const double* A = &sitePos[3 * i];
-      for (int j = i; j < nsites; ++j) {
+      {
         const TypeInfo& t2 = types[siteType[j]];
         const double* B = &sitePos[3 * j];
         int e1 = t1.element, e2 = t2.element;
@@ -663,8 +673,12 @@ struct Oracle {
         if (sepSq > negl) continue;
         double maxR = sepSq + negl + 2.0 * std::sqrt(sepSq * negl);
         if (maxR > cellSize.back()) {
-          err = "More lattice points needed for this atom overlap pair";
-          return OLC_ERR_LATTICE;
+#pragma omp critical
+          {
+            err = "More lattice points needed for this atom overlap pair";
+            status = OLC_ERR_LATTICE;
+          }
+          continue;
         }
         const int M1 = t1.nstates, M2 = t2.nstates;
         std::fill(cur.begin(), cur.end(), cplx(0, 0));
@@ -748,7 +762,8 @@ struct Oracle {
         save_pair(i, j, cur.data(), vv, cv, cc);
       }
     }
-    return OLC_OK;
+    }
+    return status;
   }
 
   // saveCurrentPair and helpers (intgSaving.F90:201-505)

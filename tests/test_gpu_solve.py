@@ -67,28 +67,60 @@ def test_gpu_packed_storage_form(case):
     assert np.abs(H - hp).max() <= 1e-10 * np.abs(hp).max() + 1e-13
 
 
+def _fused_reference(o, coeffs):
+    """The fused form's semantics on the oracle: H = ortho(KE + NP) +
+    ortho(sum_j c_j V_j), each summed operator flushed once (the reference's
+    storage form flushes |x| < 1e-10 per stored term instead)."""
+    vS, cS, ccS = o.operator(orc.OP_OVERLAP)
+    Sp = o.ortho_pack(True, vS, cS, ccS, cS)
+    ke, np_ = o.operator(orc.OP_KINETIC), o.operator(orc.OP_NUCLEAR)
+    h0 = [a + b if a is not None else None for a, b in zip(ke, np_)]
+    acc = [np.zeros_like(x) if x is not None else None for x in h0]
+    c = np.where(coeffs == 0.0, 1.0, coeffs)
+    for j in range(o.pot_dim):
+        vj = o.operator(orc.OP_ELECPOT, j)
+        for i in range(3):
+            if acc[i] is not None:
+                acc[i] += c[j] * vj[i]
+    hp = o.ortho_pack(False, h0[0], h0[1], h0[2], cS) + o.ortho_pack(False, acc[0], acc[1], acc[2], cS)
+    return orc.zhegv(hp, Sp, o.vale_dim, o.vale_dim)[0]
+
+
 @pytest.mark.gpu
 def test_scf_iteration_fused(case):
     sysm, o, packed, hp, w, ctx = case
     ctx.scf_prepare()
+    for c in (sysm.pot_coeffs, sysm.pot_coeffs * 0.5):
+        eig = ctx.scf_iteration(c, o.vale_dim)
+        assert np.abs(eig - _fused_reference(o, c)).max() <= EIG_TOL
+        # against the reference's storage form the per-term flush accounts
+        # for the difference
+        ws, _ = orc.zhegv(orc.assemble(packed, c), packed["S"], o.vale_dim, o.vale_dim)
+        assert np.abs(eig - ws).max() <= 1e-6
+
+
+@pytest.mark.gpu
+def test_scf_iteration_stored(case):
+    """Stored form: resident packed V_j summed with the coefficients."""
+    from olcao_gb300 import api
+    sysm, o, packed, hp, w, ctx = case
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
     eig = ctx.scf_iteration(sysm.pot_coeffs, o.vale_dim)
     assert np.abs(eig - w).max() <= EIG_TOL
-    # a second pass with other coefficients stays consistent
-    c2 = sysm.pot_coeffs * 0.5
-    hp2 = orc.assemble(packed, c2)
-    w2, _ = orc.zhegv(hp2, packed["S"], o.vale_dim, o.vale_dim)
-    eig2 = ctx.scf_iteration(c2, o.vale_dim)
-    assert np.abs(eig2 - w2).max() <= EIG_TOL
+    H, Sm = ctx.scf_matrices(sysm.pot_coeffs, 0)
+    assert np.abs(H - orc.unpack(hp[0], o.vale_dim)).max() <= 1e-10 * np.abs(H).max()
+    assert np.abs(Sm - orc.unpack(packed["S"][0], o.vale_dim)).max() <= 1e-10 * np.abs(Sm).max()
 
 
 @pytest.mark.gpu
 def test_zero_coefficient_rule(case):
     """A zero multiplier adds its term unscaled, as readPackedMatrixAccum does."""
+    from olcao_gb300 import api
     sysm, o, packed, hp, w, ctx = case
     c = sysm.pot_coeffs.copy()
     c[0] = 0.0
-    hp0 = orc.assemble(packed, c)
-    w0, _ = orc.zhegv(hp0, packed["S"], o.vale_dim, o.vale_dim)
-    ctx.scf_prepare()
-    eig = ctx.scf_iteration(c, o.vale_dim)
-    assert np.abs(eig - w0).max() <= EIG_TOL
+    w0, _ = orc.zhegv(orc.assemble(packed, c), packed["S"], o.vale_dim, o.vale_dim)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    assert np.abs(ctx.scf_iteration(c, o.vale_dim) - w0).max() <= EIG_TOL
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_FUSED)
+    assert np.abs(ctx.scf_iteration(c, o.vale_dim) - _fused_reference(o, c)).max() <= EIG_TOL
