@@ -226,6 +226,31 @@ int olc_profile_read(olc_context_t* ctx, int stage, int64_t* launches, double* m
 /* Kernels of this library launched so far in the process (all contexts). */
 int64_t olc_launch_count(void);
 
+/* Allocation-free variant of the generalised eigen-solve, for callers that
+ * may not allocate device memory once their SCF loop runs: a host program
+ * that reserves all device memory for its own pool at start-up, or a
+ * framework that owns the device allocator and does not let libraries call
+ * cudaMalloc/cudaFree.  This entry point has no counterpart in the reference.
+ *
+ * Same result as olc_solve_zhegv for n <= 64 (the batched in-shared-memory
+ * solver), but needs no context and allocates nothing: every pointer is
+ * DEVICE memory supplied by the caller -- packed_h / packed_s [2, n(n+1)/2, nk],
+ * eigenvalues [num_states, nk], vectors [n, num_states, nk] (may be NULL),
+ * info [nk] (LAPACK-style codes, written by the kernel).  The unpacked
+ * working copies live in one 16 MiB device array that every GPU loading the
+ * library holds until exit, so nk * n * n must not exceed 524288; larger
+ * requests are rejected with OLC_ERR_ARG and a message.
+ *
+ * The first call on a device looks up that array's device address (with
+ * the device current); make that first call before any stream capture.
+ * Work is queued on `stream` (NULL = legacy stream) and not synchronised.
+ * Calls share the array and every call overwrites all of the part it uses,
+ * so nothing is carried over between calls, but calls that overlap on the
+ * GPU (different streams, or concurrent host threads) race on it. */
+int olc_solve_zhegv_noalloc(int n, int nk, const double* packed_h, const double* packed_s,
+                            int num_states, double* eigenvalues, double* vectors,
+                            int32_t* info, void* stream);
+
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the
  * device.  kind: 1 overlap2CIntg, 2 kinetic2CIntg, 3 nuclear3CIntg,

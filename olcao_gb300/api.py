@@ -44,7 +44,7 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_ortho_pack", "olc_assemble_hamiltonian", "olc_solve_zhegv",
            "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
-           "olc_launch_count", "olc_scf_matrices")
+           "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc")
 STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve")
 
 _LIB: Optional[C.CDLL] = None
@@ -90,6 +90,7 @@ def lib() -> C.CDLL:
         for name in EXPORTS[2:]:
             getattr(L, name).restype = C.c_int
         L.olc_scf_matrices.argtypes = [vp, dp, i32, dp, dp, i32]
+        L.olc_solve_zhegv_noalloc.argtypes = [i32, i32, dp, dp, i32, dp, dp, dp, vp]
         L.olc_launch_count.restype = C.c_int64
         L.olc_launch_count.argtypes = []
         _LIB = L

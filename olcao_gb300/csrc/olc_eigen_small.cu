@@ -341,4 +341,22 @@ int solve_small_batched(olc_context* ctx, const double* h_full, const double* s_
   return OLC_OK;
 }
 
+// Launches the batched solver on full Hermitian h, s [nk][n][n] with no
+// allocation and no synchronisation (info is device memory).
+int launch_small_hegv_raw(cudaStream_t stream, const double* h_full, const double* s_full, int n,
+                          int nk, int num_states, double* eigenvalues, double* vectors,
+                          int32_t* info_dev) {
+  const size_t smem = sizeof(double) * 2 * 3 * (size_t)n * n + sizeof(double) * n + sizeof(int) * n;
+  int st;
+  if ((st = cuda_check(cudaFuncSetAttribute(small_hegv_kernel,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "smem attribute"))) return st;
+  count_launch();
+  small_hegv_kernel<<<nk, kThreads, smem, stream>>>(h_full, s_full, n, num_states, 0, eigenvalues,
+                                                    vectors, info_dev, nullptr);
+  return cuda_check(cudaGetLastError(), "small_hegv_kernel");
+}
+
+int small_solver_capacity_n() { return kSmallMaxN; }
+
 }  // namespace olc
