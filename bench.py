@@ -10,9 +10,13 @@ Monkhorst-Pack mesh (64 k-points), complex128 H(k), S(k).
 One step is one SCF iteration of the reference's secularEqnAllKP: H(k) =
 NP + KE + sum_j c_j V_j assembled from the orthogonalised, packed integrals
 (computed once by the integral kernels and kept resident in HBM, as
-OLCAOsetup stores them), then the generalised eigen-problem for every k.  The
-potential coefficients change every step.  The resident integrals (~6.7 GB)
-exceed L2, so no flush is needed between steps.
+OLCAOsetup stores them), then the generalised eigen-problem with eigenvectors
+for every k.  The potential coefficients change every step.  The resident
+integrals (~6.7 GB) exceed L2, so no flush is needed between steps.
+
+The headline is the mixed+batched form (FP32 solves, Rayleigh-Ritz with
+error-free split-BF16 tensor-core products); the same run times the plain
+FP64 GPU path and reports the largest eigenvalue difference between them.
 
 --impl reference times the CPU restatement of the same iteration (assembly +
 LAPACK zhegv per k) on the host cores, on a bounded sample of k-points.
@@ -49,6 +53,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", default="si64", choices=sorted(WORKLOADS))
     p.add_argument("--form", default="stored", choices=["stored", "fused"])
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--no-fused", action="store_true", help="skip the fused-form timing")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--cpu-sample-k", type=int, default=2)
@@ -196,6 +201,7 @@ def run_ours(args, world, rank, dist):
     n, nk, pd = ctx.vale_dim, ctx.nk, ctx.pot_dim
     nstates = n
     form = api.FORM_STORED if args.form == "stored" else api.FORM_FUSED
+    prec = api.PREC_MIXED if args.precision == "mixed" else api.PREC_FP64
 
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -211,7 +217,7 @@ def run_ours(args, world, rank, dist):
     # eigenvectors are produced every step, as solveZHEGV does for the density
     vec = torch.empty(nk, nstates, n, dtype=torch.complex128, device="cuda")
     for w in range(args.warmup):
-        ctx.scf_iteration(dco[w % 5], nstates, eig_out=eig, vectors=vec)
+        ctx.scf_iteration(dco[w % 5], nstates, eig_out=eig, vectors=vec, precision=prec)
     torch.cuda.synchronize()
     # under `ncu --profile-from-start off` only the timed steps are captured
     mark = os.environ.get("OLC_BENCH_PROFILE_TIMED") == "1"
@@ -228,7 +234,7 @@ def run_ours(args, world, rank, dist):
         torch.cuda.profiler.start()
     ev0.record(stream)
     for s in range(args.steps):
-        ctx.scf_iteration(dco[s % 5], nstates, eig_out=eig, vectors=vec)
+        ctx.scf_iteration(dco[s % 5], nstates, eig_out=eig, vectors=vec, precision=prec)
     ev1.record(stream)
     torch.cuda.synchronize()
     if mark:
@@ -244,6 +250,7 @@ def run_ours(args, world, rank, dist):
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
+    eig_main = eig.cpu().numpy().copy()
 
     # ---- e2e: public API with host buffers ------------------------------------
     host_c = [torch.from_numpy(c).pin_memory() for c in coeff_steps]
@@ -254,7 +261,7 @@ def run_ours(args, world, rank, dist):
     t0 = time.perf_counter()
     for s in range(args.steps):
         ctx.scf_iteration(host_c[s % 5].numpy(), nstates, eig_out=eig_host.numpy(),
-                          vectors=vec)
+                          vectors=vec, precision=prec)
     torch.cuda.synchronize()
     e2e = (time.perf_counter() - t0) / args.steps
     if dist:
@@ -262,16 +269,38 @@ def run_ours(args, world, rank, dist):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e = float(t.item())
 
+    # ---- plain FP64 GPU path on the same step (accuracy and speed-up) ---------
+    t_fp64 = None
+    acc = None
+    if prec == api.PREC_MIXED and world == 1:
+        last = (args.steps - 1) % 5
+        ctx.scf_iteration(dco[last], nstates, eig_out=eig, vectors=vec, precision=api.PREC_FP64)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        reps = 2
+        for r in range(reps):
+            ctx.scf_iteration(dco[last], nstates, eig_out=eig, vectors=vec,
+                              precision=api.PREC_FP64)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t_fp64 = ev0.elapsed_time(ev1) / reps / 1e3
+        w64 = eig.cpu().numpy()
+        nocc = 2 * len(full.site_type) if args.config.startswith("si") else min(nstates, 4 * len(full.site_type) // 2)
+        band = lambda w: float(2.0 * w[:, :nocc].sum() / w.shape[0])
+        acc = {"max_abs_eig_err_ha": float(np.abs(eig_main - w64).max()),
+               "band_energy_err_ha": abs(band(eig_main) - band(w64)),
+               "reference": "plain FP64 GPU path (cuSOLVER zhegvd) on the same H(k), S(k)"}
+
     # ---- fused form (integrals recomputed with the coefficients) --------------
     t_fused = None
     if rank == 0 and not args.no_fused and world == 1:
         ctxf = api.Context(sysm)
         ctxf.scf_prepare(api.PREC_FP64, api.FORM_FUSED)
-        ctxf.scf_iteration(dco[0], nstates, eig_out=eig, vectors=vec)
+        ctxf.scf_iteration(dco[0], nstates, eig_out=eig, vectors=vec, precision=prec)
         torch.cuda.synchronize()
         ev0.record(stream)
         for s in range(2):
-            ctxf.scf_iteration(dco[s], nstates, eig_out=eig, vectors=vec)
+            ctxf.scf_iteration(dco[s], nstates, eig_out=eig, vectors=vec, precision=prec)
         ev1.record(stream)
         torch.cuda.synchronize()
         t_fused = ev0.elapsed_time(ev1) / 2 / 1e3
@@ -313,9 +342,12 @@ def run_ours(args, world, rank, dist):
     line = {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": False, "scaling": "strong", "vs_baseline": None,
-            "dtype": "fp64", "data": f"synthetic seeded ({full.name}, seed {full.seed})",
+            "dtype": "fp64+fp32+bf16" if prec == api.PREC_MIXED else "fp64",
+            "data": f"synthetic seeded ({full.name}, seed {full.seed})",
             "config": {"workload": WORKLOADS[args.config], "form": args.form,
-                       "precision": "fp64 (plain path)", "n_basis": n,
+                       "precision": ("mixed: FP32 solve + split-BF16 Rayleigh-Ritz, FP64 integrals"
+                                     if prec == api.PREC_MIXED else "fp64 (plain path)"),
+                       "n_basis": n,
                        "num_kpoints": nk_total, "pot_dim": pd,
                        "l2": "resident integrals larger than L2, no flush"},
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": pd * 8,
@@ -323,6 +355,9 @@ def run_ours(args, world, rank, dist):
             "gpu_launches": int(launches),
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "t_setup_s": t_setup, "t_iter_fused_s": t_fused,
+            "t_iter_fp64_gpu_s": t_fp64,
+            "speedup_vs_fp64_gpu": (t_fp64 / (ms / 1e3)) if t_fp64 else None,
+            "accuracy": acc,
             "stages": stages}
     print(json.dumps(line), flush=True)
 

@@ -207,6 +207,13 @@ int olc_scf_iteration(olc_context_t* ctx, const double* coeffs, int precision,
 int olc_scf_matrices(olc_context_t* ctx, const double* coeffs, int kpoint,
                      double* h, double* s, int on_device);
 
+/* FP64-accurate complex product C = A B (DEVICE, column-major, m x k times
+ * k x n) formed error-free from BF16 slices on the tensor cores -- the product
+ * the mixed-precision solver (OLC_PREC_MIXED) builds its Rayleigh-Ritz
+ * matrices with.  Exposed for checking and for callers' own products. */
+int olc_split_zgemm(olc_context_t* ctx, int m, int n, int k, const double* a,
+                    const double* b, double* c);
+
 /* Stage timing (CUDA events on the context's stream) and kernel counting.
  * Stages: the integral primitives, the basis contraction, the Bloch sum and
  * scatter, the orthogonalisation (GEMMs + pack), Hamiltonian assembly, and

@@ -44,7 +44,8 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_ortho_pack", "olc_assemble_hamiltonian", "olc_solve_zhegv",
            "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
-           "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc")
+           "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
+           "olc_split_zgemm")
 STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve")
 
 _LIB: Optional[C.CDLL] = None
@@ -91,6 +92,7 @@ def lib() -> C.CDLL:
             getattr(L, name).restype = C.c_int
         L.olc_scf_matrices.argtypes = [vp, dp, i32, dp, dp, i32]
         L.olc_solve_zhegv_noalloc.argtypes = [i32, i32, dp, dp, i32, dp, dp, dp, vp]
+        L.olc_split_zgemm.argtypes = [vp, i32, i32, i32, dp, dp, dp]
         L.olc_launch_count.restype = C.c_int64
         L.olc_launch_count.argtypes = []
         _LIB = L
@@ -248,6 +250,20 @@ class Context:
 
     def scf_prepare(self, precision: int = PREC_FP64, form: int = FORM_FUSED):
         _check(lib().olc_scf_prepare(self.h, precision, form))
+
+    def split_zgemm(self, A, B):
+        """FP64-accurate complex product on the tensor cores (device tensors,
+        row-major numpy-style [rows, cols]; computed column-major inside)."""
+        torch = self.torch
+        m, k = A.shape
+        k2, n = B.shape
+        assert k == k2
+        Ac = A.t().contiguous()        # column-major storage of A
+        Bc = B.t().contiguous()
+        Cc = torch.zeros(n, m, dtype=torch.complex128, device="cuda")
+        _check(lib().olc_split_zgemm(self.h, m, n, k, Ac.data_ptr(), Bc.data_ptr(),
+                                     Cc.data_ptr()))
+        return Cc.t()
 
     def scf_matrices(self, coeffs, k: int):
         """Full Hermitian H(k), S(k) of the prepared pass, as host arrays."""

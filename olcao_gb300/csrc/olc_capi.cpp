@@ -78,6 +78,8 @@ int cuda_check(cudaError_t e, const char* what) {
 }
 
 int build_phase_table(olc_context* ctx);
+int ozaki_selftest(olc_context* ctx, int m, int n, int k, const double* A, const double* B,
+                   double* C);
 int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const double* cv,
                   const double* cc, const double* scv, double* packed, double* full,
                   const double* add);
@@ -143,6 +145,13 @@ int olc_destroy(olc_context_t* ctx) {
     cudaFree(ctx->sub_eval[i]);
     cudaStreamDestroy(ctx->sub_streams[i]);
     cudaEventDestroy(ctx->ev_join[i]);
+  }
+  for (size_t i = 0; i < ctx->mixed_streams.size(); ++i) {
+    cudaStreamSynchronize(ctx->mixed_streams[i]);
+    cusolverDnDestroy(ctx->mixed_solvers[i]);
+    cudaFree(ctx->mixed_work[i]);
+    cudaStreamDestroy(ctx->mixed_streams[i]);
+    cudaEventDestroy(ctx->mixed_join[i]);
   }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->blas) cublasDestroy(ctx->blas);
@@ -232,6 +241,13 @@ int olc_scf_matrices(olc_context_t* ctx, const double* coeffs, int kpoint, doubl
                      int on_device) {
   if (!ctx || !coeffs) return fail(OLC_ERR_ARG, "olc_scf_matrices: null argument");
   return scf_matrices(ctx, coeffs, kpoint, h, s, on_device);
+}
+
+int olc_split_zgemm(olc_context_t* ctx, int m, int n, int k, const double* a, const double* b,
+                    double* c) {
+  if (!ctx || !a || !b || !c || m < 1 || n < 1 || k < 1)
+    return fail(OLC_ERR_ARG, "olc_split_zgemm: bad argument");
+  return ozaki_selftest(ctx, m, n, k, a, b, c);
 }
 
 int olc_profile_enable(olc_context_t* ctx, int on) {

@@ -150,6 +150,13 @@ struct olc_context {
   int sub_n = 0;
   cudaEvent_t ev_fork = nullptr;
   std::vector<cudaEvent_t> ev_join;
+  // FP32 solves of the mixed-precision path
+  std::vector<cudaStream_t> mixed_streams;
+  std::vector<cusolverDnHandle_t> mixed_solvers;
+  std::vector<void*> mixed_work;
+  std::vector<cudaEvent_t> mixed_join;
+  int mixed_n = 0;
+  int mixed_lwork = 0;
   int* d_info = nullptr;
   double* d_eval = nullptr;
   // profiling

@@ -346,9 +346,34 @@ int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
   return OLC_OK;
 }
 
+int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
+                     double* eig_dev, double* vectors);
+
 int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* eigenvalues,
-               int eig_on_device, double* vectors, int32_t* info) {
+               int eig_on_device, double* vectors, int32_t* info, int precision = OLC_PREC_FP64) {
   const int n = ctx->dims.vale_dim;
+  if (precision == OLC_PREC_MIXED && n > small_solver_max_n()) {
+    int st;
+    double* eig_dev = eigenvalues;
+    double* tmp = nullptr;
+    const int nk = ctx->dims.num_kpoints;
+    if (!eig_on_device) {
+      if ((st = cuda_check(cudaMallocAsync((void**)&tmp, sizeof(double) * (size_t)num_states * nk,
+                                           ctx->stream), "malloc eigs"))) return st;
+      eig_dev = tmp;
+    }
+    st = solve_full_mixed(ctx, h, s, num_states, eig_dev, vectors);
+    if (!eig_on_device) {
+      cudaMemcpyAsync(eigenvalues, tmp, sizeof(double) * (size_t)num_states * nk,
+                      cudaMemcpyDeviceToHost, ctx->stream);
+      cudaFreeAsync(tmp, ctx->stream);
+      int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "eig copy");
+      if (!st) st = s2;
+    }
+    if (info)
+      for (int k = 0; k < nk; ++k) info[k] = 0;
+    return st;
+  }
   if (n <= small_solver_max_n()) {
     int st;
     double* eig_dev = eigenvalues;
@@ -517,7 +542,7 @@ int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num
   if ((st = build_hamiltonian(ctx, coeffs, precision, flags, h))) return st;
   cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
   st = solve_full(ctx, h, s, num_states, eigenvalues, (flags & OLC_ITER_EIG_DEVICE) ? 1 : 0,
-                  vectors, nullptr);
+                  vectors, nullptr, precision);
   cudaFreeAsync(h, ctx->stream);
   cudaFreeAsync(s, ctx->stream);
   int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "iteration sync");

@@ -1,0 +1,655 @@
+// Mixed-precision generalised eigen-solve (OLC_PREC_MIXED), for all k at once.
+//
+// The reference solves every H(k) x = e S(k) x with LAPACK zhegv in FP64
+// (solveZHEGV, interfaces.F90:73-120).  On GB300 FP64 arithmetic runs at about
+// 1 TFLOP/s while BF16 tensor-core products run above 1 PFLOP/s, so the
+// FP64-accurate answer is recovered from an FP32 solve instead:
+//
+//   1. FP32 pencil: cuSOLVER chegvd per k (concurrent streams) gives X (n x n,
+//      S-orthonormal to FP32 accuracy) and its eigenvalues.
+//   2. Rayleigh-Ritz in that basis with FP64-accurate products:
+//        Hh = X^H (H X),  Sh = X^H (S X).
+//      Each product is formed error-free from BF16 slices on the tensor cores
+//      (the splitting of Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59
+//      (2012) 95-118): every row (left operand) or column (right operand) is
+//      scaled by a power of two and cut into 6-bit integer slices, which BF16
+//      holds exactly; every slice product accumulates integers below 2^24 in
+//      FP32, hence exactly; the slice products are summed with their scales
+//      in FP64.  Complex products use the real embedding
+//      [[Ar,-Ai],[Ai,Ar]] [[Br],[Bi]].
+//   3. The pencil (Hh, Sh) is diagonal up to the FP32 error of X.  After the
+//      scaling D = diag(Sh)^(-1/2), states are grouped into clusters of close
+//      diagonal values (gap < 5e-3 Ha, at most 64 states); each cluster's
+//      block, with the rest of the spectrum folded in to second order, is
+//      solved exactly by the shared-memory Jacobi solver.  Eigenvectors are
+//      X D y.
+#include <algorithm>
+#include <cstdio>
+#include <cuda_bf16.h>
+
+#include "olc_common.h"
+#include "olc_jacobi.cuh"
+
+namespace olc {
+
+namespace {
+
+using jac::cd;
+
+constexpr double kClusterGap = 5e-3;
+constexpr int kSortMax = 8192;      // n limit of the in-shared-memory sort
+
+// ---------------------------------------------------------------------------
+// conversions
+// ---------------------------------------------------------------------------
+__global__ void to_c64_kernel(const double* __restrict__ in, float* __restrict__ out, size_t n2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// ---------------------------------------------------------------------------
+// error-free slicing
+// ---------------------------------------------------------------------------
+// Logical complex operand: element (r, c) of an (rows x cols) matrix, read
+// from a column-major source with leading dimension ld.  conj_trans reads the
+// conjugate transpose of the source.
+template <class T>
+__device__ __forceinline__ void load_c(const T* src, int ld, bool conj_trans, int r, int c,
+                                       double& re, double& im) {
+  if (!conj_trans) {
+    re = (double)src[2 * ((size_t)c * ld + r)];
+    im = (double)src[2 * ((size_t)c * ld + r) + 1];
+  } else {
+    re = (double)src[2 * ((size_t)r * ld + c)];
+    im = -(double)src[2 * ((size_t)r * ld + c) + 1];
+  }
+}
+
+// exponent e with max|x| < 2^e over a row (left operand) or column (right)
+template <class T>
+__global__ void exponent_kernel(const T* __restrict__ src, long long src_stride, int ld,
+                                bool conj_trans, int rows, int cols, bool per_row,
+                                int* __restrict__ expo, int nb) {
+  const int lines = per_row ? rows : cols;
+  const int len = per_row ? cols : rows;
+  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gwarp >= lines * nb) return;
+  const int b = gwarp / lines, line = gwarp % lines;
+  const T* s = src + (size_t)b * src_stride;
+  double mx = 0.0;
+  for (int t = lane; t < len; t += 32) {
+    double re, im;
+    if (per_row) load_c(s, ld, conj_trans, line, t, re, im);
+    else load_c(s, ld, conj_trans, t, line, re, im);
+    mx = fmax(mx, fmax(fabs(re), fabs(im)));
+  }
+  for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) {
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);      // mx = f 2^e, f in [0.5, 1): |x| < 2^e
+    else e = -1000;
+    expo[(size_t)b * lines + line] = e;
+  }
+}
+
+// Left operand (m x k complex) -> nsl slices of the real embedding
+// (2m x 2k, column-major) as BF16 integers; per-row exponents.
+template <class T>
+__global__ void slice_left_kernel(const T* __restrict__ src, long long src_stride, int ld,
+                                  bool conj_trans, int m, int k, const int* __restrict__ expo,
+                                  int nsl, int beta, __nv_bfloat16* __restrict__ out, int nb) {
+  const size_t per = (size_t)m * k;
+  const size_t total = per * nb;
+  const size_t big = (size_t)4 * m * k;   // one slice of one batch entry
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(idx / per);
+    const size_t q = idx % per;
+    const int r = (int)(q % m), c = (int)(q / m);
+    double re, im;
+    load_c(src + (size_t)b * src_stride, ld, conj_trans, r, c, re, im);
+    const int e = expo[(size_t)b * m + r];
+    double ar = ldexp(re, -e), ai = ldexp(im, -e);
+    __nv_bfloat16* o = out + (size_t)b * nsl * big;
+    const size_t M2 = 2 * (size_t)m;
+    for (int s = 0; s < nsl; ++s) {
+      const double tr = ldexp(ar, beta), ti = ldexp(ai, beta);
+      const double qr = trunc(tr), qi = trunc(ti);
+      ar = tr - qr;
+      ai = ti - qi;
+      __nv_bfloat16* os = o + (size_t)s * big;
+      const __nv_bfloat16 br = __float2bfloat16_rn((float)qr);
+      const __nv_bfloat16 bi = __float2bfloat16_rn((float)qi);
+      const __nv_bfloat16 nbi = __float2bfloat16_rn((float)-qi);
+      os[(size_t)c * M2 + r] = br;                        // [r, c]     = Ar
+      os[(size_t)(c + k) * M2 + r] = nbi;                 // [r, c+k]   = -Ai
+      os[(size_t)c * M2 + r + m] = bi;                    // [r+m, c]   = Ai
+      os[(size_t)(c + k) * M2 + r + m] = br;              // [r+m, c+k] = Ar
+    }
+  }
+}
+
+// Right operand (k x n complex) -> nsl slices of [[Br],[Bi]] (2k x n); per-column exponents.
+template <class T>
+__global__ void slice_right_kernel(const T* __restrict__ src, long long src_stride, int ld,
+                                   int k, int n, const int* __restrict__ expo, int nsl, int beta,
+                                   __nv_bfloat16* __restrict__ out, int nb) {
+  const size_t per = (size_t)k * n;
+  const size_t total = per * nb;
+  const size_t big = (size_t)2 * k * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(idx / per);
+    const size_t q = idx % per;
+    const int r = (int)(q % k), c = (int)(q / k);
+    double re, im;
+    load_c(src + (size_t)b * src_stride, ld, false, r, c, re, im);
+    const int e = expo[(size_t)b * n + c];
+    double ar = ldexp(re, -e), ai = ldexp(im, -e);
+    __nv_bfloat16* o = out + (size_t)b * nsl * big;
+    const size_t K2 = 2 * (size_t)k;
+    for (int s = 0; s < nsl; ++s) {
+      const double tr = ldexp(ar, beta), ti = ldexp(ai, beta);
+      const double qr = trunc(tr), qi = trunc(ti);
+      ar = tr - qr;
+      ai = ti - qi;
+      __nv_bfloat16* os = o + (size_t)s * big;
+      os[(size_t)c * K2 + r] = __float2bfloat16_rn((float)qr);
+      os[(size_t)c * K2 + r + k] = __float2bfloat16_rn((float)qi);
+    }
+  }
+}
+
+// C (m x n complex, FP64) (+)= 2^(e_r + f_c - beta (s + t + 2)) * G, G = [[Gr],[Gi]] (2m x n FP32)
+__global__ void ozaki_accumulate_kernel(const float* __restrict__ G, const int* __restrict__ ea,
+                                        const int* __restrict__ fb, int m, int n, int shift,
+                                        bool first, double* __restrict__ C, int nb) {
+  const size_t per = (size_t)m * n;
+  const size_t total = per * nb;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(idx / per);
+    const size_t q = idx % per;
+    const int r = (int)(q % m), c = (int)(q / m);
+    const float* g = G + (size_t)b * 2 * m * n;
+    const int sc = ea[(size_t)b * m + r] + fb[(size_t)b * n + c] - shift;
+    const double vr = ldexp((double)g[(size_t)c * 2 * m + r], sc);
+    const double vi = ldexp((double)g[(size_t)c * 2 * m + r + m], sc);
+    double* o = C + 2 * ((size_t)b * per + q);
+    if (first) {
+      o[0] = vr;
+      o[1] = vi;
+    } else {
+      o[0] += vr;
+      o[1] += vi;
+    }
+  }
+}
+
+int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32); }
+
+// Bits per slice so that a length-2k sum of slice products stays below 2^24
+// (exact in FP32): 2 beta + ceil(log2(2k)) <= 24.
+int slice_bits(int k) {
+  int lg = 0;
+  while ((1LL << lg) < 2LL * k) ++lg;
+  return std::max(1, std::min(7, (24 - lg) / 2));
+}
+int max_slices(int bits, int k) { return (bits + slice_bits(k) - 1) / slice_bits(k); }
+
+// ---------------------------------------------------------------------------
+// extraction
+// ---------------------------------------------------------------------------
+// Per k: a_i = Re Hh_ii / Re Sh_ii, sorted; clusters of consecutive values
+// closer than kClusterGap, at most jac::kMaxN states.  Writes the sorted order
+// [nk][n], the cluster starts [nk][n+1] (in sorted positions) and counts [nk].
+__global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict__ Hh,
+                                                       const double* __restrict__ Sh, int n,
+                                                       int* __restrict__ order_out,
+                                                       int* __restrict__ starts,
+                                                       int* __restrict__ counts) {
+  extern __shared__ double sortmem[];
+  int P0 = 1;
+  while (P0 < n) P0 <<= 1;
+  double* key = sortmem;
+  int* idx = reinterpret_cast<int*>(sortmem + P0);
+  const int k = blockIdx.x, tid = threadIdx.x;
+  const size_t nn = (size_t)n * n;
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int i = tid; i < P; i += blockDim.x) {
+    if (i < n) {
+      const double h = Hh[2 * ((size_t)k * nn + (size_t)i * n + i)];
+      const double s = Sh[2 * ((size_t)k * nn + (size_t)i * n + i)];
+      key[i] = h / s;
+    } else {
+      key[i] = 1e300;
+    }
+    idx[i] = i;
+  }
+  __syncthreads();
+  // bitonic sort ascending
+  for (int size = 2; size <= P; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = tid; i < P; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          if ((key[i] > key[j]) == up) {
+            const double t = key[i]; key[i] = key[j]; key[j] = t;
+            const int u = idx[i]; idx[i] = idx[j]; idx[j] = u;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = tid; i < n; i += blockDim.x) order_out[(size_t)k * n + i] = idx[i];
+  if (tid == 0) {
+    int nc = 0, cur = 0;
+    starts[(size_t)k * (n + 1)] = 0;
+    for (int i = 1; i < n; ++i) {
+      if (key[i] - key[i - 1] >= kClusterGap || i - cur >= jac::kMaxN) {
+        ++nc;
+        starts[(size_t)k * (n + 1) + nc] = i;
+        cur = i;
+      }
+    }
+    ++nc;
+    starts[(size_t)k * (n + 1) + nc] = n;
+    counts[k] = nc;
+  }
+}
+
+struct ClusterArgs {
+  const double* Hh;
+  const double* Sh;
+  const float* X;          // FP32 basis [nk][n][n] complex
+  const int* order;
+  const int* starts;
+  const int* counts;
+  int n;
+  double* w_slot;          // [nk][n] eigenvalues in sorted-slot order
+  double* v_slot;          // [nk][n][n] complex vectors in slot order (or nullptr)
+};
+
+// One CTA per (cluster, k): fold the rest of the spectrum into the cluster
+// block to second order, solve the block exactly, write eigenvalues and
+// vectors X D y.
+__global__ void __launch_bounds__(256) cluster_solve_kernel(ClusterArgs a) {
+  const int k = blockIdx.y, ci = blockIdx.x;
+  if (ci >= a.counts[k]) return;
+  const int n = a.n;
+  const size_t nn = (size_t)n * n;
+  const int s0 = a.starts[(size_t)k * (n + 1) + ci];
+  const int m = a.starts[(size_t)k * (n + 1) + ci + 1] - s0;
+  const int* ord = a.order + (size_t)k * n;
+  extern __shared__ double smem[];
+  cd* U = reinterpret_cast<cd*>(smem);
+  cd* C = U + jac::kMaxN * jac::kMaxN;
+  cd* V = C + jac::kMaxN * jac::kMaxN;
+  cd* Cp = V + jac::kMaxN * jac::kMaxN;           // [32][m] chunk of couplings
+  double* dcol = reinterpret_cast<double*>(Cp + 32 * jac::kMaxN);   // [32] denominators
+  int* cidx = reinterpret_cast<int*>(dcol + 32);                     // [m]
+  double* dsc = reinterpret_cast<double*>(cidx + jac::kMaxN);       // [m] diag scaling
+  __shared__ jac::Shared sh;
+  __shared__ double s_lc;
+  const double* H = a.Hh + 2 * (size_t)k * nn;
+  const double* S = a.Sh + 2 * (size_t)k * nn;
+  const int tid = threadIdx.x;
+  for (int p = tid; p < m; p += blockDim.x) {
+    cidx[p] = ord[s0 + p];
+    dsc[p] = 1.0 / sqrt(S[2 * ((size_t)cidx[p] * n + cidx[p])]);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int p = 0; p < m; ++p) t += H[2 * ((size_t)cidx[p] * n + cidx[p])] * dsc[p] * dsc[p];
+    s_lc = t / m;
+  }
+  __syncthreads();
+  const double lc = s_lc;
+  // cluster block of A = D Hh D and B = D Sh D
+  for (int e = tid; e < m * m; e += blockDim.x) {
+    const int p = e % m, q = e / m;
+    const size_t o = 2 * ((size_t)cidx[q] * n + cidx[p]);
+    const double sc = dsc[p] * dsc[q];
+    C[q * m + p] = {H[o] * sc, H[o + 1] * sc};
+    U[q * m + p] = {S[o] * sc, S[o + 1] * sc};
+  }
+  __syncthreads();
+  // second-order folding: C += sum_{j not in cluster} Cp_j^H Cp_j / (lc - a_j)
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int J = min(32, n - j0);
+    for (int e = tid; e < J * m; e += blockDim.x) {
+      const int jj = e / m, p = e % m;
+      const int j = j0 + jj;
+      bool inside = false;
+      for (int q = 0; q < m; ++q) inside |= (cidx[q] == j);
+      const double dj = 1.0 / sqrt(S[2 * ((size_t)j * n + j)]);
+      const size_t o = 2 * ((size_t)cidx[p] * n + j);
+      const double sc = dj * dsc[p];
+      const double ar = H[o] * sc, ai = H[o + 1] * sc;
+      const double br = S[o] * sc, bi = S[o + 1] * sc;
+      Cp[jj * m + p] = inside ? cd{0.0, 0.0} : cd{ar - lc * br, ai - lc * bi};
+      if (p == 0) {
+        const double aj = H[2 * ((size_t)j * n + j)] * dj * dj;
+        dcol[jj] = inside ? 0.0 : 1.0 / (lc - aj);
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int p = e % m, q = e / m;
+      double re = 0.0, im = 0.0;
+      for (int jj = 0; jj < J; ++jj) {
+        const cd x = Cp[jj * m + p], y = Cp[jj * m + q];
+        const double w = dcol[jj];
+        re += w * (x.x * y.x + x.y * y.y);      // conj(x) * y
+        im += w * (x.x * y.y - x.y * y.x);
+      }
+      C[q * m + p].x += re;
+      C[q * m + p].y += im;
+    }
+    __syncthreads();
+  }
+  jac::hegv_inplace(U, C, V, m, false, sh, nullptr);
+  // eigenvalues of the cluster (unsorted inside the cluster)
+  for (int i = tid; i < m; i += blockDim.x) a.w_slot[(size_t)k * n + s0 + i] = C[(size_t)i * m + i].x;
+  if (!a.v_slot) return;
+  // y = U^{-1} V (in place in V, column by column), then x = X D y
+  for (int col = tid; col < m; col += blockDim.x) {
+    for (int r = m - 1; r >= 0; --r) {
+      cd acc = V[(size_t)col * m + r];
+      for (int q = r + 1; q < m; ++q) acc = jac::csub(acc, jac::cmul(U[(size_t)q * m + r], V[(size_t)col * m + q]));
+      const double inv = 1.0 / U[(size_t)r * m + r].x;
+      V[(size_t)col * m + r] = {acc.x * inv, acc.y * inv};
+    }
+  }
+  __syncthreads();
+  const float* X = a.X + 2 * (size_t)k * nn;
+  for (int e = tid; e < n * m; e += blockDim.x) {
+    const int row = e % n, col = e / n;
+    double re = 0.0, im = 0.0;
+    for (int p = 0; p < m; ++p) {
+      const size_t o = 2 * ((size_t)cidx[p] * n + row);
+      const double xr = X[o] * dsc[p], xi = X[o + 1] * dsc[p];
+      const cd y = V[(size_t)col * m + p];
+      re += xr * y.x - xi * y.y;
+      im += xr * y.y + xi * y.x;
+    }
+    double* o = a.v_slot + 2 * ((size_t)k * nn + (size_t)(s0 + col) * n + row);
+    o[0] = re;
+    o[1] = im;
+  }
+}
+
+// Final ascending order over all clusters; gathers eigenvalues and vectors.
+__global__ void __launch_bounds__(1024) final_sort_kernel(const double* __restrict__ w_slot,
+                                                          const double* __restrict__ v_slot,
+                                                          int n, int num_states,
+                                                          double* __restrict__ eig,
+                                                          double* __restrict__ vec) {
+  extern __shared__ double sortmem[];
+  int P0 = 1;
+  while (P0 < n) P0 <<= 1;
+  double* key = sortmem;
+  int* idx = reinterpret_cast<int*>(sortmem + P0);
+  const int k = blockIdx.x, tid = threadIdx.x;
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int i = tid; i < P; i += blockDim.x) {
+    key[i] = i < n ? w_slot[(size_t)k * n + i] : 1e300;
+    idx[i] = i;
+  }
+  __syncthreads();
+  for (int size = 2; size <= P; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = tid; i < P; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          if ((key[i] > key[j]) == up) {
+            const double t = key[i]; key[i] = key[j]; key[j] = t;
+            const int u = idx[i]; idx[i] = idx[j]; idx[j] = u;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = tid; i < num_states; i += blockDim.x) eig[(size_t)k * num_states + i] = key[i];
+  if (!vec) return;
+  const size_t nn = (size_t)n * n;
+  for (size_t e = tid; e < (size_t)n * num_states; e += blockDim.x) {
+    const int row = (int)(e % n), col = (int)(e / n);
+    const double* src = v_slot + 2 * ((size_t)k * nn + (size_t)idx[col] * n + row);
+    double* dst = vec + 2 * ((size_t)k * n * num_states + e);
+    dst[0] = src[0];
+    dst[1] = src[1];
+  }
+}
+
+}  // namespace
+
+// Error-free complex product C = op(A) B for a batch (see the file comment).
+// A: logical m x k (source column-major, ld lda, conj_trans reads A^H),
+// B: k x n (ld ldb).  T = double or float sources; na/nbs slices per operand.
+template <class TA, class TB>
+int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
+                bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
+                int nb, __nv_bfloat16* wsA, __nv_bfloat16* wsB, float* G, int* ea, int* fb) {
+  cudaStream_t st = ctx->stream;
+  const int beta = slice_bits(k);
+  const int na = (bits_a + beta - 1) / beta, nbs = (bits_b + beta - 1) / beta;
+  StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
+  const int wa = (m * nb * 32 + 255) / 256, wb = (n * nb * 32 + 255) / 256;
+  exponent_kernel<TA><<<wa, 256, 0, st>>>(A, sA, lda, conjA, m, k, true, ea, nb);
+  exponent_kernel<TB><<<wb, 256, 0, st>>>(B, sB, ldb, false, k, n, false, fb, nb);
+  slice_left_kernel<TA><<<grid_for((size_t)m * k * nb), 256, 0, st>>>(A, sA, lda, conjA, m, k, ea, na, beta, wsA, nb);
+  slice_right_kernel<TB><<<grid_for((size_t)k * n * nb), 256, 0, st>>>(B, sB, ldb, k, n, fb, nbs, beta, wsB, nb);
+  scope.add_launches(4);
+  const float one = 1.0f, zero = 0.0f;
+  const long long bigA = 4LL * m * k, bigB = 2LL * k * n;
+  bool first = true;
+  const int T = (std::max(bits_a, bits_b) + beta - 1) / beta + 1;
+  for (int s = 0; s < na; ++s)
+    for (int t = 0; t < nbs; ++t) {
+      if (s + t > T) continue;
+      cublasStatus_t bs = cublasGemmStridedBatchedEx(
+          ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * m, n, 2 * k, &one, wsA + (size_t)s * bigA,
+          CUDA_R_16BF, 2 * m, (long long)na * bigA, wsB + (size_t)t * bigB, CUDA_R_16BF, 2 * k,
+          (long long)nbs * bigB, &zero, G, CUDA_R_32F, 2 * m, 2LL * m * n, nb, CUBLAS_COMPUTE_32F,
+          CUBLAS_GEMM_DEFAULT);
+      if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "BF16 slice GEMM failed");
+      ozaki_accumulate_kernel<<<grid_for((size_t)m * n * nb), 256, 0, st>>>(
+          G, ea, fb, m, n, beta * (s + t + 2), first, C, nb);
+      scope.add_launches(1);
+      first = false;
+    }
+  return cuda_check(cudaGetLastError(), "ozaki kernels");
+}
+
+// Solve every k with the mixed-precision scheme; h, s are full Hermitian
+// FP64 [nk][n][n] (not modified).
+int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
+                     double* eig_dev, double* vectors) {
+  const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
+  if (n > kSortMax) return fail(OLC_ERR_UNSUPPORTED, "mixed solver: n above 8192");
+  const size_t nn = (size_t)n * n;
+  int st;
+  cudaStream_t stream = ctx->stream;
+  // ---- 1. FP32 generalised solve per k -----------------------------------
+  float *h32 = nullptr, *s32 = nullptr, *w32 = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&w32, 4 * (size_t)n * nk, stream), "malloc w32"))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 2);
+    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
+    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
+  }
+  const int nsub = std::max(1, std::min(nk, 16));
+  if ((int)ctx->mixed_streams.size() != nsub || ctx->mixed_n != n) {
+    for (size_t i = 0; i < ctx->mixed_streams.size(); ++i) {
+      cudaStreamSynchronize(ctx->mixed_streams[i]);
+      cusolverDnDestroy(ctx->mixed_solvers[i]);
+      cudaFree(ctx->mixed_work[i]);
+      cudaStreamDestroy(ctx->mixed_streams[i]);
+      cudaEventDestroy(ctx->mixed_join[i]);
+    }
+    ctx->mixed_streams.clear(); ctx->mixed_solvers.clear(); ctx->mixed_work.clear();
+    ctx->mixed_join.clear();
+    if (!ctx->ev_fork) cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    cusolverDnHandle_t h0;
+    if (cusolverDnCreate(&h0) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
+    int lwork = 0;
+    cusolverStatus_t ss = cusolverDnChegvd_bufferSize(
+        h0, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+        reinterpret_cast<cuComplex*>(h32), n, reinterpret_cast<cuComplex*>(s32), n, w32, &lwork);
+    cusolverDnDestroy(h0);
+    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "chegvd_bufferSize failed");
+    ctx->mixed_lwork = lwork;
+    for (int i = 0; i < nsub; ++i) {
+      cudaStream_t sm;
+      cusolverDnHandle_t hs;
+      void* w = nullptr;
+      cudaEvent_t ej;
+      if ((st = cuda_check(cudaStreamCreateWithFlags(&sm, cudaStreamNonBlocking), "sub stream"))) return st;
+      if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
+      cusolverDnSetStream(hs, sm);
+      if ((st = cuda_check(cudaMalloc(&w, sizeof(cuComplex) * (size_t)lwork), "chegvd work"))) return st;
+      cudaEventCreateWithFlags(&ej, cudaEventDisableTiming);
+      ctx->mixed_streams.push_back(sm);
+      ctx->mixed_solvers.push_back(hs);
+      ctx->mixed_work.push_back(w);
+      ctx->mixed_join.push_back(ej);
+    }
+    ctx->mixed_n = n;
+  }
+  if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
+    cudaEventRecord(ctx->ev_fork, stream);
+    for (int i = 0; i < nsub; ++i) cudaStreamWaitEvent(ctx->mixed_streams[i], ctx->ev_fork, 0);
+    for (int k = 0; k < nk; ++k) {
+      const int i = k % nsub;
+      cusolverStatus_t ss = cusolverDnChegvd(
+          ctx->mixed_solvers[i], CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+          CUBLAS_FILL_MODE_UPPER, n, reinterpret_cast<cuComplex*>(h32) + (size_t)k * nn, n,
+          reinterpret_cast<cuComplex*>(s32) + (size_t)k * nn, n, w32 + (size_t)k * n,
+          reinterpret_cast<cuComplex*>(ctx->mixed_work[i]), ctx->mixed_lwork, ctx->d_info + k);
+      if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnChegvd failed");
+    }
+    for (int i = 0; i < nsub; ++i) {
+      cudaEventRecord(ctx->mixed_join[i], ctx->mixed_streams[i]);
+      cudaStreamWaitEvent(stream, ctx->mixed_join[i], 0);
+    }
+  }
+  cudaFreeAsync(s32, stream);
+  cudaFreeAsync(w32, stream);
+  const float* X = h32;   // FP32 eigenvectors, [nk][n][n] complex
+  // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
+  __nv_bfloat16 *wsA = nullptr, *wsB = nullptr;
+  float* G = nullptr;
+  int *ea = nullptr, *fb = nullptr;
+  double *Y = nullptr, *Hh = nullptr, *Sh = nullptr;
+  const int b64 = 48, b32 = 24;        // bits kept of FP64 and FP32 operands
+  const int slmax = max_slices(b64, n);
+  if ((st = cuda_check(cudaMallocAsync((void**)&wsA, 2ULL * slmax * 4 * nn * nk, stream), "malloc slices A"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&wsB, 2ULL * slmax * 2 * nn * nk, stream), "malloc slices B"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&G, 4ULL * 2 * nn * nk, stream), "malloc G"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * n * nk, stream), "malloc ea"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * n * nk, stream), "malloc fb"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&Y, 16ULL * nn * nk, stream), "malloc Y"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&Hh, 16ULL * nn * nk, stream), "malloc Hh"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&Sh, 16ULL * nn * nk, stream), "malloc Sh"))) return st;
+  const long long snn = (long long)nn * 2;
+  // Y = H X ; Hh = X^H Y
+  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk,
+                                       wsA, wsB, G, ea, fb))) return st;
+  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Hh, nk,
+                                       wsA, wsB, G, ea, fb))) return st;
+  // Y = S X ; Sh = X^H Y
+  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, s, snn, n, false, b64, X, snn, n, b32, Y, nk,
+                                       wsA, wsB, G, ea, fb))) return st;
+  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Sh, nk,
+                                       wsA, wsB, G, ea, fb))) return st;
+  cudaFreeAsync(wsA, stream);
+  cudaFreeAsync(wsB, stream);
+  cudaFreeAsync(G, stream);
+  cudaFreeAsync(ea, stream);
+  cudaFreeAsync(fb, stream);
+  cudaFreeAsync(Y, stream);
+  // ---- 3. clusters and their exact solves -----------------------------------
+  int *order = nullptr, *starts = nullptr, *counts = nullptr;
+  double *w_slot = nullptr, *v_slot = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&order, 4ULL * n * nk, stream), "malloc order"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&starts, 4ULL * (n + 1) * nk, stream), "malloc starts"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&counts, 4ULL * nk, stream), "malloc counts"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&w_slot, 8ULL * n * nk, stream), "malloc w"))) return st;
+  if (vectors && (st = cuda_check(cudaMallocAsync((void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
+    int P = 1;
+    while (P < n) P <<= 1;
+    const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
+    if ((st = cuda_check(cudaFuncSetAttribute(cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sortmem), "smem attribute"))) return st;
+    if ((st = cuda_check(cudaFuncSetAttribute(final_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sortmem), "smem attribute"))) return st;
+    cluster_kernel<<<nk, 1024, sortmem, stream>>>(Hh, Sh, n, order, starts, counts);
+    ClusterArgs ca{Hh, Sh, X, order, starts, counts, n, w_slot, v_slot};
+    const size_t smem = sizeof(cd) * (3 * jac::kMaxN * jac::kMaxN + 32 * jac::kMaxN) +
+                        sizeof(double) * 32 + sizeof(int) * jac::kMaxN + sizeof(double) * jac::kMaxN;
+    if ((st = cuda_check(cudaFuncSetAttribute(cluster_solve_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "smem attribute"))) return st;
+    cluster_solve_kernel<<<dim3(n, nk), 256, smem, stream>>>(ca);
+    final_sort_kernel<<<nk, 1024, sortmem, stream>>>(w_slot, v_slot, n, num_states, eig_dev, vectors);
+  }
+  st = cuda_check(cudaGetLastError(), "extraction kernels");
+  cudaFreeAsync(order, stream);
+  cudaFreeAsync(starts, stream);
+  cudaFreeAsync(counts, stream);
+  cudaFreeAsync(w_slot, stream);
+  if (v_slot) cudaFreeAsync(v_slot, stream);
+  cudaFreeAsync(Hh, stream);
+  cudaFreeAsync(Sh, stream);
+  cudaFreeAsync(h32, stream);
+  std::vector<int> hinfo(nk);
+  cudaMemcpyAsync(hinfo.data(), ctx->d_info, sizeof(int) * nk, cudaMemcpyDeviceToHost, stream);
+  int s2 = cuda_check(cudaStreamSynchronize(stream), "mixed solve sync");
+  if (st) return st;
+  if (s2) return s2;
+  for (int k = 0; k < nk; ++k) {
+    if (hinfo[k] > n) return fail(OLC_ERR_NOT_PD, "overlap matrix not positive definite (FP32 factorisation)");
+    if (hinfo[k] != 0) return fail(OLC_ERR_EIGEN, "FP32 eigen-solver did not converge");
+  }
+  return OLC_OK;
+}
+
+// Error-free product check entry (tests): C = A B for one complex FP64 pair.
+int ozaki_selftest(olc_context* ctx, int m, int n, int k, const double* A, const double* B,
+                   double* C) {
+  __nv_bfloat16 *wsA = nullptr, *wsB = nullptr;
+  float* G = nullptr;
+  int *ea = nullptr, *fb = nullptr;
+  int st;
+  cudaStream_t stream = ctx->stream;
+  const int sl = max_slices(53, k);
+  if ((st = cuda_check(cudaMallocAsync((void**)&wsA, 2ULL * sl * 4 * m * k, stream), "malloc"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&wsB, 2ULL * sl * 2 * k * n, stream), "malloc"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&G, 4ULL * 2 * m * n, stream), "malloc"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * m, stream), "malloc"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * n, stream), "malloc"))) return st;
+  st = ozaki_zgemm<double, double>(ctx, m, n, k, A, 0, m, false, 53, B, 0, k, 53, C, 1, wsA, wsB, G, ea, fb);
+  cudaFreeAsync(wsA, stream);
+  cudaFreeAsync(wsB, stream);
+  cudaFreeAsync(G, stream);
+  cudaFreeAsync(ea, stream);
+  cudaFreeAsync(fb, stream);
+  int s2 = cuda_check(cudaStreamSynchronize(stream), "ozaki selftest sync");
+  return st ? st : s2;
+}
+
+}  // namespace olc
