@@ -225,7 +225,8 @@ typedef enum {
   OLC_STAGE_ORTHO = 3,
   OLC_STAGE_ASSEMBLE = 4,
   OLC_STAGE_SOLVE = 5,
-  OLC_NUM_STAGES = 6
+  OLC_STAGE_REFINE = 6,        /* mixed precision: split products + extraction */
+  OLC_NUM_STAGES = 7
 } olc_stage_t;
 int olc_profile_enable(olc_context_t* ctx, int on);
 int olc_profile_reset(olc_context_t* ctx);

@@ -46,7 +46,7 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
            "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
            "olc_split_zgemm")
-STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve")
+STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve", "refine")
 
 _LIB: Optional[C.CDLL] = None
 

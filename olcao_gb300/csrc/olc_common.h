@@ -7,7 +7,9 @@
 #include <cusolverDn.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "olcao_gpu.h"
@@ -198,6 +200,25 @@ int dalloc(olc_context* ctx, T** p, size_t count) {
   ctx->allocations.push_back(q);
   *p = static_cast<T*>(q);
   return OLC_OK;
+}
+
+// Runs fn(i) for i in [0, nthreads) on separate host threads with `device`
+// current.  Library calls that block their host thread (cuSOLVER's divide and
+// conquer waits on the device) overlap only when issued from different
+// threads.  Returns the first non-zero status.
+inline int parallel_host(int nthreads, int device, const std::function<int(int)>& fn) {
+  std::vector<int> status(nthreads, 0);
+  std::vector<std::thread> pool;
+  pool.reserve(nthreads);
+  for (int i = 0; i < nthreads; ++i)
+    pool.emplace_back([&, i]() {
+      cudaSetDevice(device);
+      status[i] = fn(i);
+    });
+  for (auto& t : pool) t.join();
+  for (int v : status)
+    if (v) return v;
+  return 0;
 }
 
 // host set-up (olc_setup.cpp)

@@ -306,24 +306,27 @@ int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
   StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
   cudaEventRecord(ctx->ev_fork, ctx->stream);
   for (int i = 0; i < nsub; ++i) cudaStreamWaitEvent(ctx->sub_streams[i], ctx->ev_fork, 0);
-  for (int k = 0; k < nk; ++k) {
-    const int i = k % nsub;
+  st = parallel_host(nsub, ctx->device, [&](int i) -> int {
     cudaStream_t sm = ctx->sub_streams[i];
-    auto* H = reinterpret_cast<cuDoubleComplex*>(h) + (size_t)k * nn;
-    auto* S = reinterpret_cast<cuDoubleComplex*>(s) + (size_t)k * nn;
-    cusolverStatus_t ss = cusolverDnZhegvd(ctx->sub_solvers[i], CUSOLVER_EIG_TYPE_1,
-                                           CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, H,
-                                           n, S, n, ctx->sub_eval[i],
-                                           reinterpret_cast<cuDoubleComplex*>(ctx->sub_work[i]),
-                                           lwork, ctx->d_info + k);
-    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnZhegvd failed");
-    scope.add_launches(1);
-    gather_eigs_kernel<<<(num_states + 127) / 128, 128, 0, sm>>>(ctx->sub_eval[i], n, num_states,
-                                                                 k, eig_dev);
-    if (vectors)
-      cudaMemcpyAsync(vectors + 2 * (size_t)k * n * num_states, H,
-                      sizeof(cuDoubleComplex) * (size_t)n * num_states, cudaMemcpyDeviceToDevice, sm);
-  }
+    for (int k = i; k < nk; k += nsub) {
+      auto* H = reinterpret_cast<cuDoubleComplex*>(h) + (size_t)k * nn;
+      auto* S = reinterpret_cast<cuDoubleComplex*>(s) + (size_t)k * nn;
+      cusolverStatus_t ss = cusolverDnZhegvd(ctx->sub_solvers[i], CUSOLVER_EIG_TYPE_1,
+                                             CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+                                             H, n, S, n, ctx->sub_eval[i],
+                                             reinterpret_cast<cuDoubleComplex*>(ctx->sub_work[i]),
+                                             lwork, ctx->d_info + k);
+      if (ss != CUSOLVER_STATUS_SUCCESS) return OLC_ERR_CUDA;
+      gather_eigs_kernel<<<(num_states + 127) / 128, 128, 0, sm>>>(ctx->sub_eval[i], n, num_states,
+                                                                   k, eig_dev);
+      if (vectors)
+        cudaMemcpyAsync(vectors + 2 * (size_t)k * n * num_states, H,
+                        sizeof(cuDoubleComplex) * (size_t)n * num_states, cudaMemcpyDeviceToDevice, sm);
+    }
+    return 0;
+  });
+  scope.add_launches(nk);
+  if (st) return fail(st, "cusolverDnZhegvd failed");
   for (int i = 0; i < nsub; ++i) {
     cudaEventRecord(ctx->ev_join[i], ctx->sub_streams[i]);
     cudaStreamWaitEvent(ctx->stream, ctx->ev_join[i], 0);

@@ -12,17 +12,22 @@
 //      Each product is formed error-free from BF16 slices on the tensor cores
 //      (the splitting of Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59
 //      (2012) 95-118): every row (left operand) or column (right operand) is
-//      scaled by a power of two and cut into 6-bit integer slices, which BF16
+//      scaled by a power of two and cut into short integer slices, which BF16
 //      holds exactly; every slice product accumulates integers below 2^24 in
 //      FP32, hence exactly; the slice products are summed with their scales
 //      in FP64.  Complex products use the real embedding
 //      [[Ar,-Ai],[Ai,Ar]] [[Br],[Bi]].
-//   3. The pencil (Hh, Sh) is diagonal up to the FP32 error of X.  After the
+//   3. Sh = I + E with E ~ 1e-5: the Loewdin transform (I+F)^H Hh (I+F),
+//      F = -E/2 + 3E^2/8, makes the pencil standard to O(E^3); since F is
+//      small its products need only FP32 GEMMs.  The basis becomes X (I+F).
+//   4. The pencil is diagonal up to the FP32 error of X.  After the
 //      scaling D = diag(Sh)^(-1/2), states are grouped into clusters of close
 //      diagonal values (gap < 5e-3 Ha, at most 64 states); each cluster's
 //      block, with the rest of the spectrum folded in to second order, is
 //      solved exactly by the shared-memory Jacobi solver.  Eigenvectors are
 //      X D y.
+// The slices hold ceil(bits / beta) integer chunks per operand, beta chosen
+// so that a length-2k sum of products stays exact in FP32 (6 bits at k = 832).
 #include <algorithm>
 #include <cstdio>
 #include <cuda_bf16.h>
@@ -162,28 +167,28 @@ __global__ void slice_right_kernel(const T* __restrict__ src, long long src_stri
   }
 }
 
-// C (m x n complex, FP64) (+)= 2^(e_r + f_c - beta (s + t + 2)) * G, G = [[Gr],[Gi]] (2m x n FP32)
+// C (m x n complex, FP64) (+)= 2^(e_r + f_c - shift) * G, G = [[Gr],[Gi]] (2m x n FP32);
+// blockIdx.y is the batch entry.
 __global__ void ozaki_accumulate_kernel(const float* __restrict__ G, const int* __restrict__ ea,
                                         const int* __restrict__ fb, int m, int n, int shift,
-                                        bool first, double* __restrict__ C, int nb) {
-  const size_t per = (size_t)m * n;
-  const size_t total = per * nb;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (size_t)gridDim.x * blockDim.x) {
-    const int b = (int)(idx / per);
-    const size_t q = idx % per;
-    const int r = (int)(q % m), c = (int)(q / m);
-    const float* g = G + (size_t)b * 2 * m * n;
-    const int sc = ea[(size_t)b * m + r] + fb[(size_t)b * n + c] - shift;
-    const double vr = ldexp((double)g[(size_t)c * 2 * m + r], sc);
-    const double vi = ldexp((double)g[(size_t)c * 2 * m + r + m], sc);
-    double* o = C + 2 * ((size_t)b * per + q);
+                                        bool first, double* __restrict__ C) {
+  const int b = blockIdx.y;
+  const int per = m * n;
+  const float* g = G + (size_t)b * 2 * per;
+  const int* e = ea + (size_t)b * m;
+  const int* f = fb + (size_t)b * n;
+  double* o = C + 2 * (size_t)b * per;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < per; q += gridDim.x * blockDim.x) {
+    const int r = q % m, c = q / m;
+    const double sc = ldexp(1.0, e[r] + f[c] - shift);
+    const double vr = (double)g[(size_t)c * 2 * m + r] * sc;
+    const double vi = (double)g[(size_t)c * 2 * m + r + m] * sc;
     if (first) {
-      o[0] = vr;
-      o[1] = vi;
+      o[2 * (size_t)q] = vr;
+      o[2 * (size_t)q + 1] = vi;
     } else {
-      o[0] += vr;
-      o[1] += vi;
+      o[2 * (size_t)q] += vr;
+      o[2 * (size_t)q + 1] += vi;
     }
   }
 }
@@ -275,8 +280,10 @@ struct ClusterArgs {
 };
 
 // One CTA per (cluster, k): fold the rest of the spectrum into the cluster
-// block to second order, solve the block exactly, write eigenvalues and
-// vectors X D y.
+// block to second order -- F1 = sum_j c_j^H c_j / (lc - a_j) at the cluster's
+// mean energy lc, with its first-order energy dependence through
+// D2 = sum_j c_j^H c_j / (lc - a_j)^2, i.e. (A + F1 + lc D2) y = E (B + D2) y --
+// solve that block exactly, write eigenvalues and vectors X D y.
 __global__ void __launch_bounds__(256) cluster_solve_kernel(ClusterArgs a) {
   const int k = blockIdx.y, ci = blockIdx.x;
   if (ci >= a.counts[k]) return;
@@ -341,15 +348,21 @@ __global__ void __launch_bounds__(256) cluster_solve_kernel(ClusterArgs a) {
     __syncthreads();
     for (int e = tid; e < m * m; e += blockDim.x) {
       const int p = e % m, q = e / m;
-      double re = 0.0, im = 0.0;
+      double re = 0.0, im = 0.0, re2 = 0.0, im2 = 0.0;
       for (int jj = 0; jj < J; ++jj) {
         const cd x = Cp[jj * m + p], y = Cp[jj * m + q];
-        const double w = dcol[jj];
-        re += w * (x.x * y.x + x.y * y.y);      // conj(x) * y
-        im += w * (x.x * y.y - x.y * y.x);
+        const double w = dcol[jj], xr = x.x * y.x + x.y * y.y, xi = x.x * y.y - x.y * y.x;  // conj(x) y
+        re += w * xr;
+        im += w * xi;
+        re2 += w * w * xr;
+        im2 += w * w * xi;
       }
-      C[q * m + p].x += re;
-      C[q * m + p].y += im;
+      // fold at energy lc plus its first-order energy dependence:
+      // (A + F1 + lc D2) y = E (B + D2) y
+      C[q * m + p].x += re + lc * re2;
+      C[q * m + p].y += im + lc * im2;
+      U[q * m + p].x += re2;
+      U[q * m + p].y += im2;
     }
     __syncthreads();
   }
@@ -364,6 +377,16 @@ __global__ void __launch_bounds__(256) cluster_solve_kernel(ClusterArgs a) {
       for (int q = r + 1; q < m; ++q) acc = jac::csub(acc, jac::cmul(U[(size_t)q * m + r], V[(size_t)col * m + q]));
       const double inv = 1.0 / U[(size_t)r * m + r].x;
       V[(size_t)col * m + r] = {acc.x * inv, acc.y * inv};
+    }
+    // the generalised block normalises y to y^H (B + D2) y = 1; the basis is
+    // orthonormal, so the vector itself is brought to unit norm
+    double nrm = 0.0;
+    for (int r = 0; r < m; ++r) nrm += V[(size_t)col * m + r].x * V[(size_t)col * m + r].x +
+                                       V[(size_t)col * m + r].y * V[(size_t)col * m + r].y;
+    const double sc = 1.0 / sqrt(nrm);
+    for (int r = 0; r < m; ++r) {
+      V[(size_t)col * m + r].x *= sc;
+      V[(size_t)col * m + r].y *= sc;
     }
   }
   __syncthreads();
@@ -382,6 +405,28 @@ __global__ void __launch_bounds__(256) cluster_solve_kernel(ClusterArgs a) {
     o[0] = re;
     o[1] = im;
   }
+}
+
+// Rayleigh quotients of the refined vectors: w_i = Re(x_i^H (H x_i)) / Re(x_i^H (S x_i)),
+// one warp per (vector, k).
+__global__ void rayleigh_kernel(const double* __restrict__ Xs, const double* __restrict__ HX,
+                                const double* __restrict__ SX, int n, int nk,
+                                double* __restrict__ w) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (gw >= n * nk) return;
+  const int k = gw / n, i = gw % n;
+  const size_t o = 2 * ((size_t)k * n * n + (size_t)i * n);
+  double num = 0.0, den = 0.0;
+  for (int r = lane; r < n; r += 32) {
+    const double xr = Xs[o + 2 * r], xi = Xs[o + 2 * r + 1];
+    num += xr * HX[o + 2 * r] + xi * HX[o + 2 * r + 1];
+    den += xr * SX[o + 2 * r] + xi * SX[o + 2 * r + 1];
+  }
+  for (int off = 16; off; off >>= 1) {
+    num += __shfl_xor_sync(0xffffffffu, num, off);
+    den += __shfl_xor_sync(0xffffffffu, den, off);
+  }
+  if (lane == 0) w[(size_t)k * n + i] = num / den;
 }
 
 // Final ascending order over all clusters; gathers eigenvalues and vectors.
@@ -439,9 +484,9 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
                 int nb, __nv_bfloat16* wsA, __nv_bfloat16* wsB, float* G, int* ea, int* fb) {
   cudaStream_t st = ctx->stream;
+  StageScope scope(ctx, OLC_STAGE_REFINE, 0);
   const int beta = slice_bits(k);
   const int na = (bits_a + beta - 1) / beta, nbs = (bits_b + beta - 1) / beta;
-  StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
   const int wa = (m * nb * 32 + 255) / 256, wb = (n * nb * 32 + 255) / 256;
   exponent_kernel<TA><<<wa, 256, 0, st>>>(A, sA, lda, conjA, m, k, true, ea, nb);
   exponent_kernel<TB><<<wb, 256, 0, st>>>(B, sB, ldb, false, k, n, false, fb, nb);
@@ -450,23 +495,137 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
   scope.add_launches(4);
   const float one = 1.0f, zero = 0.0f;
   const long long bigA = 4LL * m * k, bigB = 2LL * k * n;
-  bool first = true;
+  // products with equal s + t share their scale; up to `group` of them sum
+  // exactly in FP32 before the FP64 accumulation
+  const double qmax = (double)((1 << beta) - 1);
+  const int group = std::max(1, (int)((double)(1 << 24) / (2.0 * k * qmax * qmax)));
   const int T = (std::max(bits_a, bits_b) + beta - 1) / beta + 1;
-  for (int s = 0; s < na; ++s)
-    for (int t = 0; t < nbs; ++t) {
-      if (s + t > T) continue;
+  const dim3 agrid((unsigned)std::min<size_t>(((size_t)m * n + 255) / 256, 152 * 4), (unsigned)nb);
+  bool first = true;
+  for (int d = 0; d <= T; ++d) {
+    int in_group = 0;
+    for (int s = 0; s < na; ++s) {
+      const int t = d - s;
+      if (t < 0 || t >= nbs) continue;
+      const float* beta_g = in_group ? &one : &zero;
       cublasStatus_t bs = cublasGemmStridedBatchedEx(
           ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * m, n, 2 * k, &one, wsA + (size_t)s * bigA,
           CUDA_R_16BF, 2 * m, (long long)na * bigA, wsB + (size_t)t * bigB, CUDA_R_16BF, 2 * k,
-          (long long)nbs * bigB, &zero, G, CUDA_R_32F, 2 * m, 2LL * m * n, nb, CUBLAS_COMPUTE_32F,
+          (long long)nbs * bigB, beta_g, G, CUDA_R_32F, 2 * m, 2LL * m * n, nb, CUBLAS_COMPUTE_32F,
           CUBLAS_GEMM_DEFAULT);
       if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "BF16 slice GEMM failed");
-      ozaki_accumulate_kernel<<<grid_for((size_t)m * n * nb), 256, 0, st>>>(
-          G, ea, fb, m, n, beta * (s + t + 2), first, C, nb);
+      if (++in_group == group) {
+        ozaki_accumulate_kernel<<<agrid, 256, 0, st>>>(G, ea, fb, m, n, beta * (d + 2), first, C);
+        scope.add_launches(1);
+        first = false;
+        in_group = 0;
+      }
+    }
+    if (in_group) {
+      ozaki_accumulate_kernel<<<agrid, 256, 0, st>>>(G, ea, fb, m, n, beta * (d + 2), first, C);
       scope.add_launches(1);
       first = false;
     }
+  }
   return cuda_check(cudaGetLastError(), "ozaki kernels");
+}
+
+namespace {
+
+// E = Sh - I (FP32), and the FP32 copy of Hh
+__global__ void loewdin_prep_kernel(const double* __restrict__ Hh, const double* __restrict__ Sh,
+                                    int n, size_t total, float* __restrict__ E,
+                                    float* __restrict__ H32) {
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = idx % ((size_t)n * n);
+    const int row = (int)(r % n), col = (int)(r / n);
+    E[2 * idx] = (float)(Sh[2 * idx] - (row == col ? 1.0 : 0.0));
+    E[2 * idx + 1] = (float)Sh[2 * idx + 1];
+    H32[2 * idx] = (float)Hh[2 * idx];
+    H32[2 * idx + 1] = (float)Hh[2 * idx + 1];
+  }
+}
+
+// F = -E/2 + (3/8) E2   (in place in E2)
+__global__ void loewdin_f_kernel(const float* __restrict__ E, float* __restrict__ E2, size_t n2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2;
+       i += (size_t)gridDim.x * blockDim.x)
+    E2[i] = -0.5f * E[i] + 0.375f * E2[i];
+}
+
+// out (FP64) = base (FP64) + add (FP32); optional FP32 copy of the sum
+__global__ void add_f32_kernel(double* __restrict__ out, const double* __restrict__ base,
+                               const float* __restrict__ add, float* __restrict__ copy32,
+                               size_t n2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double v = base[i] + (double)add[i];
+    out[i] = v;
+    if (copy32) copy32[i] = (float)v;
+  }
+}
+
+// Sh := I (the transformed pencil is standard)
+__global__ void set_identity_kernel(double* __restrict__ S, int n, size_t total) {
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = idx % ((size_t)n * n);
+    S[2 * idx] = ((int)(r % n) == (int)(r / n)) ? 1.0 : 0.0;
+    S[2 * idx + 1] = 0.0;
+  }
+}
+
+__global__ void add_f32_inplace_kernel(float* __restrict__ X, const float* __restrict__ add,
+                                       size_t n2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2;
+       i += (size_t)gridDim.x * blockDim.x)
+    X[i] += add[i];
+}
+
+}  // namespace
+
+// Hh := (I+F)^H Hh (I+F), Sh := I, X := X (I+F) with F = -E/2 + 3E^2/8, E = Sh - I.
+int loewdin(olc_context* ctx, int n, int nk, double* Hh, double* Sh, float* X) {
+  cudaStream_t stream = ctx->stream;
+  const size_t nn = (size_t)n * n, total = nn * nk;
+  float *E = nullptr, *F = nullptr, *H32 = nullptr, *T = nullptr;
+  int st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&E, 8 * total, stream), "malloc E"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&F, 8 * total, stream), "malloc F"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&H32, 8 * total, stream), "malloc H32"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&T, 8 * total, stream), "malloc T"))) return st;
+  StageScope scope(ctx, OLC_STAGE_REFINE, 0);
+  loewdin_prep_kernel<<<grid_for(total), 256, 0, stream>>>(Hh, Sh, n, total, E, H32);
+  const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+  auto* Ec = reinterpret_cast<cuComplex*>(E);
+  auto* Fc = reinterpret_cast<cuComplex*>(F);
+  auto* Hc = reinterpret_cast<cuComplex*>(H32);
+  auto* Tc = reinterpret_cast<cuComplex*>(T);
+  auto* Xc = reinterpret_cast<cuComplex*>(X);
+  const long long sn = (long long)nn;
+  auto gemm = [&](cublasOperation_t ta, const cuComplex* A, const cuComplex* B, cuComplex* C) {
+    return cublasCgemmStridedBatched(ctx->blas, ta, CUBLAS_OP_N, n, n, n, &one, A, n, sn, B, n, sn,
+                                     &zero, C, n, sn, nk);
+  };
+  if (gemm(CUBLAS_OP_N, Ec, Ec, Fc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm E^2 failed");
+  loewdin_f_kernel<<<grid_for(2 * total), 256, 0, stream>>>(E, F, 2 * total);
+  // W = Hh + Hh F  (into Hh, FP32 copy into H32)
+  if (gemm(CUBLAS_OP_N, Hc, Fc, Tc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm HF failed");
+  add_f32_kernel<<<grid_for(2 * total), 256, 0, stream>>>(Hh, Hh, T, H32, 2 * total);
+  // Hh' = W + F^H W
+  if (gemm(CUBLAS_OP_C, Fc, Hc, Tc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm FW failed");
+  add_f32_kernel<<<grid_for(2 * total), 256, 0, stream>>>(Hh, Hh, T, nullptr, 2 * total);
+  // X' = X + X F
+  if (gemm(CUBLAS_OP_N, Xc, Fc, Tc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm XF failed");
+  add_f32_inplace_kernel<<<grid_for(2 * total), 256, 0, stream>>>(X, T, 2 * total);
+  set_identity_kernel<<<grid_for(total), 256, 0, stream>>>(Sh, n, total);
+  scope.add_launches(6);
+  cudaFreeAsync(E, stream);
+  cudaFreeAsync(F, stream);
+  cudaFreeAsync(H32, stream);
+  cudaFreeAsync(T, stream);
+  return cuda_check(cudaGetLastError(), "loewdin kernels");
 }
 
 // Solve every k with the mixed-precision scheme; h, s are full Hermitian
@@ -488,7 +647,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
     to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
   }
-  const int nsub = std::max(1, std::min(nk, 16));
+  const int nsub = std::max(1, std::min(nk, 32));
   if ((int)ctx->mixed_streams.size() != nsub || ctx->mixed_n != n) {
     for (size_t i = 0; i < ctx->mixed_streams.size(); ++i) {
       cudaStreamSynchronize(ctx->mixed_streams[i]);
@@ -531,15 +690,19 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
     cudaEventRecord(ctx->ev_fork, stream);
     for (int i = 0; i < nsub; ++i) cudaStreamWaitEvent(ctx->mixed_streams[i], ctx->ev_fork, 0);
-    for (int k = 0; k < nk; ++k) {
-      const int i = k % nsub;
-      cusolverStatus_t ss = cusolverDnChegvd(
-          ctx->mixed_solvers[i], CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-          CUBLAS_FILL_MODE_UPPER, n, reinterpret_cast<cuComplex*>(h32) + (size_t)k * nn, n,
-          reinterpret_cast<cuComplex*>(s32) + (size_t)k * nn, n, w32 + (size_t)k * n,
-          reinterpret_cast<cuComplex*>(ctx->mixed_work[i]), ctx->mixed_lwork, ctx->d_info + k);
-      if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnChegvd failed");
-    }
+    const float* hbase = h32;
+    st = parallel_host(nsub, ctx->device, [&](int i) -> int {
+      for (int k = i; k < nk; k += nsub) {
+        cusolverStatus_t ss = cusolverDnChegvd(
+            ctx->mixed_solvers[i], CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+            CUBLAS_FILL_MODE_UPPER, n, reinterpret_cast<cuComplex*>(const_cast<float*>(hbase)) + (size_t)k * nn, n,
+            reinterpret_cast<cuComplex*>(s32) + (size_t)k * nn, n, w32 + (size_t)k * n,
+            reinterpret_cast<cuComplex*>(ctx->mixed_work[i]), ctx->mixed_lwork, ctx->d_info + k);
+        if (ss != CUSOLVER_STATUS_SUCCESS) return OLC_ERR_CUDA;
+      }
+      return 0;
+    });
+    if (st) return fail(st, "cusolverDnChegvd failed");
     for (int i = 0; i < nsub; ++i) {
       cudaEventRecord(ctx->mixed_join[i], ctx->mixed_streams[i]);
       cudaStreamWaitEvent(stream, ctx->mixed_join[i], 0);
@@ -547,7 +710,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   }
   cudaFreeAsync(s32, stream);
   cudaFreeAsync(w32, stream);
-  const float* X = h32;   // FP32 eigenvectors, [nk][n][n] complex
+  float* X = h32;         // FP32 eigenvectors, [nk][n][n] complex
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
   __nv_bfloat16 *wsA = nullptr, *wsB = nullptr;
   float* G = nullptr;
@@ -580,16 +743,20 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   cudaFreeAsync(ea, stream);
   cudaFreeAsync(fb, stream);
   cudaFreeAsync(Y, stream);
-  // ---- 3. clusters and their exact solves -----------------------------------
+  // ---- 3. Loewdin transform: Sh = I + E  ->  (I+F)^H Hh (I+F), F = -E/2 + 3E^2/8
+  // so that the pencil is standard; the products with the small F need only
+  // FP32 (their relative error times |F| ~ 1e-5 is far below FP64 needs)
+  if ((st = loewdin(ctx, n, nk, Hh, Sh, h32))) return st;
+  // ---- 4. clusters and their exact solves -----------------------------------
   int *order = nullptr, *starts = nullptr, *counts = nullptr;
   double *w_slot = nullptr, *v_slot = nullptr;
   if ((st = cuda_check(cudaMallocAsync((void**)&order, 4ULL * n * nk, stream), "malloc order"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&starts, 4ULL * (n + 1) * nk, stream), "malloc starts"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&counts, 4ULL * nk, stream), "malloc counts"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&w_slot, 8ULL * n * nk, stream), "malloc w"))) return st;
-  if (vectors && (st = cuda_check(cudaMallocAsync((void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
+    StageScope scope(ctx, OLC_STAGE_REFINE, 3);
     int P = 1;
     while (P < n) P <<= 1;
     const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
@@ -605,14 +772,21 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "smem attribute"))) return st;
     cluster_solve_kernel<<<dim3(n, nk), 256, smem, stream>>>(ca);
+  }
+  if ((st = cuda_check(cudaGetLastError(), "extraction kernels"))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_REFINE, 1);
+    int P = 1;
+    while (P < n) P <<= 1;
+    const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
     final_sort_kernel<<<nk, 1024, sortmem, stream>>>(w_slot, v_slot, n, num_states, eig_dev, vectors);
   }
-  st = cuda_check(cudaGetLastError(), "extraction kernels");
+  st = cuda_check(cudaGetLastError(), "final sort");
   cudaFreeAsync(order, stream);
   cudaFreeAsync(starts, stream);
   cudaFreeAsync(counts, stream);
   cudaFreeAsync(w_slot, stream);
-  if (v_slot) cudaFreeAsync(v_slot, stream);
+  cudaFreeAsync(v_slot, stream);
   cudaFreeAsync(Hh, stream);
   cudaFreeAsync(Sh, stream);
   cudaFreeAsync(h32, stream);
