@@ -117,7 +117,9 @@ typedef enum {
 
 typedef enum {
   OLC_PREC_FP64 = 0,      /* plain FP64 path                                  */
-  OLC_PREC_MIXED = 1      /* FP32 far-shell terms, FP64 near-shell and Boys   */
+  OLC_PREC_MIXED = 1      /* eigen-solve in FP32 refined by error-free split-BF16
+                             Rayleigh-Ritz products to FP64-grade eigenvalues;
+                             integrals and assembly stay FP64                 */
 } olc_precision_t;
 
 typedef struct olc_context olc_context_t;
