@@ -20,12 +20,14 @@
 //   3. Sh = I + E with E ~ 1e-5: the Loewdin transform (I+F)^H Hh (I+F),
 //      F = -E/2 + 3E^2/8, makes the pencil standard to O(E^3); since F is
 //      small its products need only FP32 GEMMs.  The basis becomes X (I+F).
-//   4. The pencil is diagonal up to the FP32 error of X.  After the
-//      scaling D = diag(Sh)^(-1/2), states are grouped into clusters of close
-//      diagonal values (gap < 5e-3 Ha, at most 64 states); each cluster's
-//      block, with the rest of the spectrum folded in to second order, is
-//      solved exactly by the shared-memory Jacobi solver.  Eigenvectors are
-//      X D y.
+//   4. The pencil is now standard and diagonal up to the FP32 error of X.
+//      States are grouped into clusters of close diagonal values (gap
+//      < 5e-3 Ha, at most 64 states); the rest of the spectrum is folded into
+//      each cluster to second order with its first-order energy dependence.
+//      A single state gets its shifted energy in closed form; a larger
+//      cluster is diagonalised by an FP32 Jacobi solver after the shift by
+//      its mean energy (the shifted block's norm is the cluster width, so
+//      FP32 rounding stays near 1e-8 Ha).  Eigenvectors are X z.
 // The slices hold ceil(bits / beta) integer chunks per operand, beta chosen
 // so that a length-2k sum of products stays exact in FP32 (6 bits at k = 832).
 #include <algorithm>
@@ -207,35 +209,45 @@ int max_slices(int bits, int k) { return (bits + slice_bits(k) - 1) / slice_bits
 // ---------------------------------------------------------------------------
 // extraction
 // ---------------------------------------------------------------------------
-// Per k: a_i = Re Hh_ii / Re Sh_ii, sorted; clusters of consecutive values
-// closer than kClusterGap, at most jac::kMaxN states.  Writes the sorted order
-// [nk][n], the cluster starts [nk][n+1] (in sorted positions) and counts [nk].
-__global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict__ Hh,
-                                                       const double* __restrict__ Sh, int n,
-                                                       int* __restrict__ order_out,
-                                                       int* __restrict__ starts,
-                                                       int* __restrict__ counts) {
+constexpr int kMaxCluster = 64;     // states per exactly-solved cluster
+constexpr int kSmallCluster = 16;   // clusters up to this size use the small kernel
+
+struct ClusterLists {
+  int* order;      // [nk][n] state held by each sorted slot
+  int* pos;        // [nk][n] sorted slot of each state
+  double* diag;    // [nk][n] a_j = Hh_jj
+  int* csize;      // [nk][n] size of the cluster holding each slot
+  int4* small;     // (k, first slot, size, 0): clusters of 2..kSmallCluster states
+  int4* large;     // clusters above kSmallCluster states
+  int* counters;   // [4] small count, large count, small next, large next
+  int cap;         // capacity of each list
+};
+
+// Per k (one CTA): a_j = Re Hh_jj (the basis is orthonormal after the Loewdin
+// step), sorted ascending; clusters are runs of consecutive values closer than
+// kClusterGap.  A run longer than kMaxCluster is cut at its widest gap.  Fills
+// the per-k arrays of L and appends every cluster of two or more states to a
+// work list.
+__global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict__ Hh, int n,
+                                                       ClusterLists L) {
   extern __shared__ double sortmem[];
-  int P0 = 1;
-  while (P0 < n) P0 <<= 1;
-  double* key = sortmem;
-  int* idx = reinterpret_cast<int*>(sortmem + P0);
-  const int k = blockIdx.x, tid = threadIdx.x;
-  const size_t nn = (size_t)n * n;
   int P = 1;
   while (P < n) P <<= 1;
+  double* key = sortmem;
+  int* idx = reinterpret_cast<int*>(sortmem + P);
+  const int k = blockIdx.x, tid = threadIdx.x;
+  const size_t nn = (size_t)n * n;
   for (int i = tid; i < P; i += blockDim.x) {
     if (i < n) {
       const double h = Hh[2 * ((size_t)k * nn + (size_t)i * n + i)];
-      const double s = Sh[2 * ((size_t)k * nn + (size_t)i * n + i)];
-      key[i] = h / s;
+      key[i] = h;
+      L.diag[(size_t)k * n + i] = h;
     } else {
       key[i] = 1e300;
     }
     idx[i] = i;
   }
   __syncthreads();
-  // bitonic sort ascending
   for (int size = 2; size <= P; size <<= 1)
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
       for (int i = tid; i < P; i += blockDim.x) {
@@ -250,183 +262,352 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict_
       }
       __syncthreads();
     }
-  for (int i = tid; i < n; i += blockDim.x) order_out[(size_t)k * n + i] = idx[i];
+  for (int i = tid; i < n; i += blockDim.x) {
+    L.order[(size_t)k * n + i] = idx[i];
+    L.pos[(size_t)k * n + idx[i]] = i;
+  }
   if (tid == 0) {
-    int nc = 0, cur = 0;
-    starts[(size_t)k * (n + 1)] = 0;
-    for (int i = 1; i < n; ++i) {
-      if (key[i] - key[i - 1] >= kClusterGap || i - cur >= jac::kMaxN) {
-        ++nc;
-        starts[(size_t)k * (n + 1) + nc] = i;
+    auto close = [&](int s0, int s1) {
+      const int m = s1 - s0;
+      for (int s = s0; s < s1; ++s) L.csize[(size_t)k * n + s] = m;
+      if (m > 1) {
+        const bool sm = m <= kSmallCluster;
+        const int at = atomicAdd(L.counters + (sm ? 0 : 1), 1);
+        if (at < L.cap) (sm ? L.small : L.large)[at] = make_int4(k, s0, m, 0);
+      }
+    };
+    int cur = 0;
+    for (int i = 1; i <= n; ++i) {
+      if (i == n || key[i] - key[i - 1] >= kClusterGap) {
+        close(cur, i);
         cur = i;
+      } else if (i - cur >= kMaxCluster) {
+        // slots cur..i form a run of kMaxCluster + 1: end the cluster at the
+        // widest gap inside it
+        int g = cur + 1;
+        for (int t = cur + 2; t <= i; ++t)
+          if (key[t] - key[t - 1] > key[g] - key[g - 1]) g = t;
+        close(cur, g);
+        cur = g;
       }
     }
-    ++nc;
-    starts[(size_t)k * (n + 1) + nc] = n;
-    counts[k] = nc;
   }
 }
 
-struct ClusterArgs {
-  const double* Hh;
-  const double* Sh;
-  const float* X;          // FP32 basis [nk][n][n] complex
-  const int* order;
-  const int* starts;
-  const int* counts;
-  int n;
-  double* w_slot;          // [nk][n] eigenvalues in sorted-slot order
-  double* v_slot;          // [nk][n][n] complex vectors in slot order (or nullptr)
+// One warp per single-state cluster: the rest of the spectrum folded in to
+// second order with its first-order energy dependence,
+//   E = a_p + F1 (1 - D2),  F1 = sum_j |A_jp|^2 / (a_p - a_j),
+//                           D2 = sum_j |A_jp|^2 / (a_p - a_j)^2,
+// and the basis vector as eigenvector.  The couplings A_jp are ~1e-6 of H
+// (the basis diagonalises H to FP32 accuracy), so F1 and D2 need only FP32.
+__global__ void __launch_bounds__(256) singleton_kernel(const double* __restrict__ Hh,
+                                                        const float* __restrict__ X,
+                                                        ClusterLists L, int n, int nk,
+                                                        double* __restrict__ w_slot,
+                                                        double* __restrict__ v_slot) {
+  const int gw = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (gw >= n * nk) return;
+  const int k = gw / n, slot = gw % n;
+  if (L.csize[(size_t)k * n + slot] != 1) return;
+  const size_t nn = (size_t)n * n;
+  const int p = L.order[(size_t)k * n + slot];
+  const double* diag = L.diag + (size_t)k * n;
+  const double ap = diag[p];
+  const double* col = Hh + 2 * ((size_t)k * nn + (size_t)p * n);
+  float f1 = 0.f, d2 = 0.f;
+  for (int j = lane; j < n; j += 32) {
+    const double dlt = ap - diag[j];
+    if (j == p || fabs(dlt) < 1e-9) continue;
+    const float w = 1.0f / (float)dlt;
+    const float ar = (float)col[2 * j], ai = (float)col[2 * j + 1];
+    const float a2 = ar * ar + ai * ai;
+    f1 += a2 * w;
+    d2 += a2 * w * w;
+  }
+  for (int o = 16; o; o >>= 1) {
+    f1 += __shfl_xor_sync(0xffffffffu, f1, o);
+    d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+  }
+  if (lane == 0) w_slot[(size_t)k * n + slot] = ap + (double)f1 * (1.0 - (double)d2);
+  if (!v_slot) return;
+  const float* x = X + 2 * ((size_t)k * nn + (size_t)p * n);
+  double* o = v_slot + 2 * ((size_t)k * nn + (size_t)slot * n);
+  for (int r = lane; r < n; r += 32) {
+    const float2 v = reinterpret_cast<const float2*>(x)[r];
+    o[2 * r] = v.x;
+    o[2 * r + 1] = v.y;
+  }
+}
+
+template <int MAXM>
+struct ClusterSmem {
+  float2 C[MAXM * MAXM];     // A - lc I + F1, then diag = eigenvalue shifts
+  float2 V[MAXM * MAXM];     // eigenvectors z
+  float2 D[MAXM * MAXM];     // D2
+  float2 Cp[32 * MAXM];      // [32][m] couplings A_jp of one chunk of j
+  float w[32];               // 1 / (lc - a_j) of the chunk (0 inside the cluster)
+  int cidx[MAXM];
+  float red[32];
+  float off, fro;
+  int item, rotated;
+  double lc;
+  int pp[MAXM / 2], qq[MAXM / 2];
+  float c[MAXM / 2], s[MAXM / 2], phx[MAXM / 2], phy[MAXM / 2];
 };
 
-// One CTA per (cluster, k): fold the rest of the spectrum into the cluster
-// block to second order -- F1 = sum_j c_j^H c_j / (lc - a_j) at the cluster's
-// mean energy lc, with its first-order energy dependence through
-// D2 = sum_j c_j^H c_j / (lc - a_j)^2, i.e. (A + F1 + lc D2) y = E (B + D2) y --
-// solve that block exactly, write eigenvalues and vectors X D y.
-__global__ void __launch_bounds__(256) cluster_solve_kernel(ClusterArgs a) {
-  const int k = blockIdx.y, ci = blockIdx.x;
-  if (ci >= a.counts[k]) return;
-  const int n = a.n;
-  const size_t nn = (size_t)n * n;
-  const int s0 = a.starts[(size_t)k * (n + 1) + ci];
-  const int m = a.starts[(size_t)k * (n + 1) + ci + 1] - s0;
-  const int* ord = a.order + (size_t)k * n;
-  extern __shared__ double smem[];
-  cd* U = reinterpret_cast<cd*>(smem);
-  cd* C = U + jac::kMaxN * jac::kMaxN;
-  cd* V = C + jac::kMaxN * jac::kMaxN;
-  cd* Cp = V + jac::kMaxN * jac::kMaxN;           // [32][m] chunk of couplings
-  double* dcol = reinterpret_cast<double*>(Cp + 32 * jac::kMaxN);   // [32] denominators
-  int* cidx = reinterpret_cast<int*>(dcol + 32);                     // [m]
-  double* dsc = reinterpret_cast<double*>(cidx + jac::kMaxN);       // [m] diag scaling
-  __shared__ jac::Shared sh;
-  __shared__ double s_lc;
-  const double* H = a.Hh + 2 * (size_t)k * nn;
-  const double* S = a.Sh + 2 * (size_t)k * nn;
+__device__ __forceinline__ float block_sum(float v, float* red, float* out) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    *out = t;
+  }
+  __syncthreads();
+  return *out;
+}
+
+// Standard Hermitian eigen-solve of the m x m FP32 block S.C by parallel
+// cyclic Jacobi (round-robin pairs, the rotation of LAPACK's zheev-free
+// two-sided scheme: J = diag(1, e^{-i phi}) R(theta)); S.V accumulates the
+// rotations.  The block is a shift of a cluster of nearly equal energies, so
+// its norm is the cluster width: entries below 3e-8 of the Frobenius norm are
+// left alone and the sweeps stop once no rotation is applied.
+template <int MAXM>
+__device__ void jacobi_f32(ClusterSmem<MAXM>& S, int m) {
   const int tid = threadIdx.x;
-  for (int p = tid; p < m; p += blockDim.x) {
-    cidx[p] = ord[s0 + p];
-    dsc[p] = 1.0 / sqrt(S[2 * ((size_t)cidx[p] * n + cidx[p])]);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double t = 0.0;
-    for (int p = 0; p < m; ++p) t += H[2 * ((size_t)cidx[p] * n + cidx[p])] * dsc[p] * dsc[p];
-    s_lc = t / m;
-  }
-  __syncthreads();
-  const double lc = s_lc;
-  // cluster block of A = D Hh D and B = D Sh D
-  for (int e = tid; e < m * m; e += blockDim.x) {
-    const int p = e % m, q = e / m;
-    const size_t o = 2 * ((size_t)cidx[q] * n + cidx[p]);
-    const double sc = dsc[p] * dsc[q];
-    C[q * m + p] = {H[o] * sc, H[o + 1] * sc};
-    U[q * m + p] = {S[o] * sc, S[o + 1] * sc};
-  }
-  __syncthreads();
-  // second-order folding: C += sum_{j not in cluster} Cp_j^H Cp_j / (lc - a_j)
-  for (int j0 = 0; j0 < n; j0 += 32) {
-    const int J = min(32, n - j0);
-    for (int e = tid; e < J * m; e += blockDim.x) {
-      const int jj = e / m, p = e % m;
-      const int j = j0 + jj;
-      bool inside = false;
-      for (int q = 0; q < m; ++q) inside |= (cidx[q] == j);
-      const double dj = 1.0 / sqrt(S[2 * ((size_t)j * n + j)]);
-      const size_t o = 2 * ((size_t)cidx[p] * n + j);
-      const double sc = dj * dsc[p];
-      const double ar = H[o] * sc, ai = H[o + 1] * sc;
-      const double br = S[o] * sc, bi = S[o + 1] * sc;
-      Cp[jj * m + p] = inside ? cd{0.0, 0.0} : cd{ar - lc * br, ai - lc * bi};
-      if (p == 0) {
-        const double aj = H[2 * ((size_t)j * n + j)] * dj * dj;
-        dcol[jj] = inside ? 0.0 : 1.0 / (lc - aj);
-      }
-    }
+  for (int e = tid; e < m * m; e += blockDim.x) S.V[e] = make_float2((e % m) == (e / m) ? 1.f : 0.f, 0.f);
+  float fro = 0.f;
+  for (int e = tid; e < m * m; e += blockDim.x) fro += S.C[e].x * S.C[e].x + S.C[e].y * S.C[e].y;
+  fro = sqrtf(block_sum(fro, S.red, &S.fro));
+  const float tiny = 3e-8f * fro + 1e-30f;
+  const int mm = (m % 2) ? m + 1 : m;
+  const int half = mm / 2;
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    if (tid == 0) S.rotated = 0;
     __syncthreads();
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int p = e % m, q = e / m;
-      double re = 0.0, im = 0.0, re2 = 0.0, im2 = 0.0;
-      for (int jj = 0; jj < J; ++jj) {
-        const cd x = Cp[jj * m + p], y = Cp[jj * m + q];
-        const double w = dcol[jj], xr = x.x * y.x + x.y * y.y, xi = x.x * y.y - x.y * y.x;  // conj(x) y
-        re += w * xr;
-        im += w * xi;
-        re2 += w * w * xr;
-        im2 += w * w * xi;
+    for (int round = 0; round < mm - 1; ++round) {
+      if (tid < half) {
+        const int pi = tid;
+        int p, q;
+        if (pi == 0) { p = round % (mm - 1); q = mm - 1; }
+        else { p = (round + pi) % (mm - 1); q = (round - pi + (mm - 1)) % (mm - 1); }
+        if (p > q) { const int t = p; p = q; q = t; }
+        float c = 1.f, s = 0.f, phx = 1.f, phy = 0.f;
+        if (q < m) {
+          const float2 cpq = S.C[q * m + p];
+          const float b = hypotf(cpq.x, cpq.y);
+          if (b > tiny) {
+            const float app = S.C[p * m + p].x, aqq = S.C[q * m + q].x;
+            const float th = (aqq - app) / (2.f * b);
+            const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(th * th + 1.f));
+            c = rsqrtf(t * t + 1.f);
+            s = t * c;
+            phx = cpq.x / b;
+            phy = -cpq.y / b;
+            S.rotated = 1;
+          }
+        }
+        S.pp[pi] = p; S.qq[pi] = q; S.c[pi] = c; S.s[pi] = s; S.phx[pi] = phx; S.phy[pi] = phy;
       }
-      // fold at energy lc plus its first-order energy dependence:
-      // (A + F1 + lc D2) y = E (B + D2) y
-      C[q * m + p].x += re + lc * re2;
-      C[q * m + p].y += im + lc * im2;
-      U[q * m + p].x += re2;
-      U[q * m + p].y += im2;
+      __syncthreads();
+      // columns: C <- C J, V <- V J
+      for (int e = tid; e < half * m; e += blockDim.x) {
+        const int pi = e / m, r = e % m;
+        const int p = S.pp[pi], q = S.qq[pi];
+        if (q >= m || S.s[pi] == 0.f) continue;
+        const float c = S.c[pi], s = S.s[pi], hx = S.phx[pi], hy = S.phy[pi];
+        {
+          const float2 xp = S.C[p * m + r], xq = S.C[q * m + r];
+          const float eqx = hx * xq.x - hy * xq.y, eqy = hx * xq.y + hy * xq.x;
+          S.C[p * m + r] = make_float2(c * xp.x - s * eqx, c * xp.y - s * eqy);
+          S.C[q * m + r] = make_float2(s * xp.x + c * eqx, s * xp.y + c * eqy);
+        }
+        {
+          const float2 xp = S.V[p * m + r], xq = S.V[q * m + r];
+          const float eqx = hx * xq.x - hy * xq.y, eqy = hx * xq.y + hy * xq.x;
+          S.V[p * m + r] = make_float2(c * xp.x - s * eqx, c * xp.y - s * eqy);
+          S.V[q * m + r] = make_float2(s * xp.x + c * eqx, s * xp.y + c * eqy);
+        }
+      }
+      __syncthreads();
+      // rows: C <- J^H C
+      for (int e = tid; e < half * m; e += blockDim.x) {
+        const int pi = e / m, col = e % m;
+        const int p = S.pp[pi], q = S.qq[pi];
+        if (q >= m || S.s[pi] == 0.f) continue;
+        const float c = S.c[pi], s = S.s[pi], hx = S.phx[pi], hy = -S.phy[pi];
+        const float2 xp = S.C[col * m + p], xq = S.C[col * m + q];
+        const float eqx = hx * xq.x - hy * xq.y, eqy = hx * xq.y + hy * xq.x;
+        S.C[col * m + p] = make_float2(c * xp.x - s * eqx, c * xp.y - s * eqy);
+        S.C[col * m + q] = make_float2(s * xp.x + c * eqx, s * xp.y + c * eqy);
+      }
+      __syncthreads();
     }
+    const int rotated = S.rotated;
     __syncthreads();
-  }
-  jac::hegv_inplace(U, C, V, m, false, sh, nullptr);
-  // eigenvalues of the cluster (unsorted inside the cluster)
-  for (int i = tid; i < m; i += blockDim.x) a.w_slot[(size_t)k * n + s0 + i] = C[(size_t)i * m + i].x;
-  if (!a.v_slot) return;
-  // y = U^{-1} V (in place in V, column by column), then x = X D y
-  for (int col = tid; col < m; col += blockDim.x) {
-    for (int r = m - 1; r >= 0; --r) {
-      cd acc = V[(size_t)col * m + r];
-      for (int q = r + 1; q < m; ++q) acc = jac::csub(acc, jac::cmul(U[(size_t)q * m + r], V[(size_t)col * m + q]));
-      const double inv = 1.0 / U[(size_t)r * m + r].x;
-      V[(size_t)col * m + r] = {acc.x * inv, acc.y * inv};
-    }
-    // the generalised block normalises y to y^H (B + D2) y = 1; the basis is
-    // orthonormal, so the vector itself is brought to unit norm
-    double nrm = 0.0;
-    for (int r = 0; r < m; ++r) nrm += V[(size_t)col * m + r].x * V[(size_t)col * m + r].x +
-                                       V[(size_t)col * m + r].y * V[(size_t)col * m + r].y;
-    const double sc = 1.0 / sqrt(nrm);
-    for (int r = 0; r < m; ++r) {
-      V[(size_t)col * m + r].x *= sc;
-      V[(size_t)col * m + r].y *= sc;
-    }
-  }
-  __syncthreads();
-  const float* X = a.X + 2 * (size_t)k * nn;
-  for (int e = tid; e < n * m; e += blockDim.x) {
-    const int row = e % n, col = e / n;
-    double re = 0.0, im = 0.0;
-    for (int p = 0; p < m; ++p) {
-      const size_t o = 2 * ((size_t)cidx[p] * n + row);
-      const double xr = X[o] * dsc[p], xi = X[o + 1] * dsc[p];
-      const cd y = V[(size_t)col * m + p];
-      re += xr * y.x - xi * y.y;
-      im += xr * y.y + xi * y.x;
-    }
-    double* o = a.v_slot + 2 * ((size_t)k * nn + (size_t)(s0 + col) * n + row);
-    o[0] = re;
-    o[1] = im;
+    if (!rotated) break;
   }
 }
 
-// Rayleigh quotients of the refined vectors: w_i = Re(x_i^H (H x_i)) / Re(x_i^H (S x_i)),
-// one warp per (vector, k).
-__global__ void rayleigh_kernel(const double* __restrict__ Xs, const double* __restrict__ HX,
-                                const double* __restrict__ SX, int n, int nk,
-                                double* __restrict__ w) {
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (gw >= n * nk) return;
-  const int k = gw / n, i = gw % n;
-  const size_t o = 2 * ((size_t)k * n * n + (size_t)i * n);
-  double num = 0.0, den = 0.0;
-  for (int r = lane; r < n; r += 32) {
-    const double xr = Xs[o + 2 * r], xi = Xs[o + 2 * r + 1];
-    num += xr * HX[o + 2 * r] + xi * HX[o + 2 * r + 1];
-    den += xr * SX[o + 2 * r] + xi * SX[o + 2 * r + 1];
+// Clusters of two or more states, one work item per CTA at a time (items taken
+// from an atomic counter).  With lc the cluster's mean energy and
+// F1 = sum_j A_.j A_j. / (lc - a_j), D2 = sum_j A_.j A_j. / (lc - a_j)^2 over
+// the states j outside the cluster, the folded pencil is
+//   (A - lc I + F1) y = (E - lc) (I + D2) y,
+// solved as the standard problem (A - lc I + F1) z = mu z in FP32 (its norm is
+// the cluster width, so FP32 rounding stays below 1e-8 Ha) with the
+// first-order effect of D2, E = lc + mu (1 - z^H D2 z).  Eigenvectors X z.
+template <int MAXM>
+__global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float* __restrict__ X,
+                                     ClusterLists L, const int4* __restrict__ list,
+                                     const int* __restrict__ count, int* __restrict__ next, int n,
+                                     double* __restrict__ w_slot, double* __restrict__ v_slot) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  ClusterSmem<MAXM>& S = *reinterpret_cast<ClusterSmem<MAXM>*>(smraw);
+  const int tid = threadIdx.x;
+  const size_t nn = (size_t)n * n;
+  const int total = min(*count, L.cap);
+  constexpr int TP = (MAXM + 3) / 4;          // 4 x 4 tiles per side
+  for (;;) {
+    if (tid == 0) S.item = atomicAdd(next, 1);
+    __syncthreads();
+    const int item = S.item;
+    if (item >= total) break;
+    const int4 it = list[item];
+    const int k = it.x, s0 = it.y, m = it.z;
+    const double* H = Hh + 2 * (size_t)k * nn;
+    const double* diag = L.diag + (size_t)k * n;
+    const int* pos = L.pos + (size_t)k * n;
+    for (int p = tid; p < m; p += blockDim.x) S.cidx[p] = L.order[(size_t)k * n + s0 + p];
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int p = 0; p < m; ++p) t += diag[S.cidx[p]];
+      S.lc = t / m;
+    }
+    __syncthreads();
+    const double lc = S.lc;
+    // ---- fold the outside states: 4 x 4 tile of (p, q) per thread -----------
+    const int tp = tid % TP, tq = tid / TP;
+    const bool own = tq < TP && 4 * tp < m && 4 * tq < m;
+    float fr[4][4], fi[4][4], dr[4][4], di[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) fr[a][b] = fi[a][b] = dr[a][b] = di[a][b] = 0.f;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+      const int J = min(32, n - j0);
+      for (int e = tid; e < 32 * m; e += blockDim.x) {
+        const int jj = e % 32, p = e / 32;
+        float2 v = make_float2(0.f, 0.f);
+        if (jj < J) {
+          const int j = j0 + jj;
+          if ((unsigned)(pos[j] - s0) >= (unsigned)m) {
+            const double* src = H + 2 * ((size_t)S.cidx[p] * n + j);   // A(j, p)
+            v = make_float2((float)src[0], (float)src[1]);
+          }
+        }
+        S.Cp[jj * MAXM + p] = v;
+      }
+      for (int jj = tid; jj < 32; jj += blockDim.x) {
+        float w = 0.f;
+        if (jj < J) {
+          const int j = j0 + jj;
+          const double dlt = lc - diag[j];
+          if ((unsigned)(pos[j] - s0) >= (unsigned)m && fabs(dlt) >= 1e-9) w = 1.0f / (float)dlt;
+        }
+        S.w[jj] = w;
+      }
+      __syncthreads();
+      if (own) {
+        for (int jj = 0; jj < J; ++jj) {
+          const float w = S.w[jj], w2 = w * w;
+          float2 x[4], y[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            x[a] = S.Cp[jj * MAXM + min(4 * tp + a, MAXM - 1)];
+            y[a] = S.Cp[jj * MAXM + min(4 * tq + a, MAXM - 1)];
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              // conj(A(j,p)) A(j,q) = A(p,j) A(j,q)
+              const float tr = x[a].x * y[b].x + x[a].y * y[b].y;
+              const float ti = x[a].x * y[b].y - x[a].y * y[b].x;
+              fr[a][b] += w * tr;
+              fi[a][b] += w * ti;
+              dr[a][b] += w2 * tr;
+              di[a][b] += w2 * ti;
+            }
+        }
+      }
+      __syncthreads();
+    }
+    // ---- the shifted block and D2 ------------------------------------------
+    if (own) {
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int p = 4 * tp + a, q = 4 * tq + b;
+          if (p < m && q < m) {
+            const double* src = H + 2 * ((size_t)S.cidx[q] * n + S.cidx[p]);   // A(p, q)
+            const double re = src[0] - (p == q ? lc : 0.0);
+            S.C[q * m + p] = make_float2((float)re + fr[a][b], (p == q) ? 0.f : (float)src[1] + fi[a][b]);
+            S.D[q * m + p] = make_float2(dr[a][b], (p == q) ? 0.f : di[a][b]);
+          }
+        }
+    }
+    __syncthreads();
+    jacobi_f32<MAXM>(S, m);
+    // ---- eigenvalues: E = lc + mu (1 - z^H D2 z) ------------------------------
+    for (int i = tid; i < m; i += blockDim.x) {
+      float dre = 0.f;
+      for (int q = 0; q < m; ++q) {
+        float2 acc = make_float2(0.f, 0.f);      // (D2 z)_q... row q of D times z
+        for (int p = 0; p < m; ++p) {
+          const float2 d = S.D[p * m + q], z = S.V[i * m + p];
+          acc.x += d.x * z.x - d.y * z.y;
+          acc.y += d.x * z.y + d.y * z.x;
+        }
+        const float2 zq = S.V[i * m + q];
+        dre += zq.x * acc.x + zq.y * acc.y;      // Re conj(z_q) (D z)_q
+      }
+      const double mu = S.C[i * m + i].x;
+      w_slot[(size_t)k * n + s0 + i] = lc + mu * (1.0 - (double)dre);
+    }
+    // ---- eigenvectors x_i = X z_i ---------------------------------------------
+    if (v_slot) {
+      const float2* Xk = reinterpret_cast<const float2*>(X) + (size_t)k * nn;
+      for (int i0 = 0; i0 < m; i0 += 8) {
+        const int I = min(8, m - i0);
+        for (int row = tid; row < n; row += blockDim.x) {
+          float ar[8], ai[8];
+#pragma unroll
+          for (int b = 0; b < 8; ++b) ar[b] = ai[b] = 0.f;
+          for (int p = 0; p < m; ++p) {
+            const float2 xv = Xk[(size_t)S.cidx[p] * n + row];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+              const float2 z = S.V[min(i0 + b, m - 1) * m + p];
+              ar[b] += xv.x * z.x - xv.y * z.y;
+              ai[b] += xv.x * z.y + xv.y * z.x;
+            }
+          }
+          for (int b = 0; b < I; ++b) {
+            double* o = v_slot + 2 * ((size_t)k * nn + (size_t)(s0 + i0 + b) * n + row);
+            o[0] = ar[b];
+            o[1] = ai[b];
+          }
+        }
+      }
+    }
+    __syncthreads();
   }
-  for (int off = 16; off; off >>= 1) {
-    num += __shfl_xor_sync(0xffffffffu, num, off);
-    den += __shfl_xor_sync(0xffffffffu, den, off);
-  }
-  if (lane == 0) w[(size_t)k * n + i] = num / den;
 }
 
 // Final ascending order over all clusters; gathers eigenvalues and vectors.
@@ -748,15 +929,20 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   // FP32 (their relative error times |F| ~ 1e-5 is far below FP64 needs)
   if ((st = loewdin(ctx, n, nk, Hh, Sh, h32))) return st;
   // ---- 4. clusters and their exact solves -----------------------------------
-  int *order = nullptr, *starts = nullptr, *counts = nullptr;
+  ClusterLists L{};
+  L.cap = (n / 2 + 1) * nk;
   double *w_slot = nullptr, *v_slot = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&order, 4ULL * n * nk, stream), "malloc order"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&starts, 4ULL * (n + 1) * nk, stream), "malloc starts"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&counts, 4ULL * nk, stream), "malloc counts"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.order, 4ULL * n * nk, stream), "malloc order"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.pos, 4ULL * n * nk, stream), "malloc pos"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.csize, 4ULL * n * nk, stream), "malloc csize"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.diag, 8ULL * n * nk, stream), "malloc diag"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.small, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.large, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&L.counters, 4 * sizeof(int), stream), "malloc counters"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&w_slot, 8ULL * n * nk, stream), "malloc w"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
+  if (vectors && (st = cuda_check(cudaMallocAsync((void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_REFINE, 3);
+    StageScope scope(ctx, OLC_STAGE_REFINE, 4);
     int P = 1;
     while (P < n) P <<= 1;
     const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
@@ -764,14 +950,21 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
                                               (int)sortmem), "smem attribute"))) return st;
     if ((st = cuda_check(cudaFuncSetAttribute(final_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sortmem), "smem attribute"))) return st;
-    cluster_kernel<<<nk, 1024, sortmem, stream>>>(Hh, Sh, n, order, starts, counts);
-    ClusterArgs ca{Hh, Sh, X, order, starts, counts, n, w_slot, v_slot};
-    const size_t smem = sizeof(cd) * (3 * jac::kMaxN * jac::kMaxN + 32 * jac::kMaxN) +
-                        sizeof(double) * 32 + sizeof(int) * jac::kMaxN + sizeof(double) * jac::kMaxN;
-    if ((st = cuda_check(cudaFuncSetAttribute(cluster_solve_kernel,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    if ((st = cuda_check(cudaMemsetAsync(L.counters, 0, 4 * sizeof(int), stream), "memset"))) return st;
+    cluster_kernel<<<nk, 1024, sortmem, stream>>>(Hh, n, L);
+    singleton_kernel<<<(int)(((size_t)n * nk * 32 + 255) / 256), 256, 0, stream>>>(Hh, X, L, n, nk, w_slot,
+                                                                                  v_slot);
+    const size_t sm_small = sizeof(ClusterSmem<kSmallCluster>), sm_large = sizeof(ClusterSmem<kMaxCluster>);
+    if ((st = cuda_check(cudaFuncSetAttribute(cluster_solve_kernel<kSmallCluster>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_small),
                          "smem attribute"))) return st;
-    cluster_solve_kernel<<<dim3(n, nk), 256, smem, stream>>>(ca);
+    if ((st = cuda_check(cudaFuncSetAttribute(cluster_solve_kernel<kMaxCluster>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_large),
+                         "smem attribute"))) return st;
+    cluster_solve_kernel<kSmallCluster><<<152 * 8, 128, sm_small, stream>>>(
+        Hh, X, L, L.small, L.counters + 0, L.counters + 2, n, w_slot, v_slot);
+    cluster_solve_kernel<kMaxCluster><<<152 * 2, 256, sm_large, stream>>>(
+        Hh, X, L, L.large, L.counters + 1, L.counters + 3, n, w_slot, v_slot);
   }
   if ((st = cuda_check(cudaGetLastError(), "extraction kernels"))) return st;
   {
@@ -782,11 +975,15 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     final_sort_kernel<<<nk, 1024, sortmem, stream>>>(w_slot, v_slot, n, num_states, eig_dev, vectors);
   }
   st = cuda_check(cudaGetLastError(), "final sort");
-  cudaFreeAsync(order, stream);
-  cudaFreeAsync(starts, stream);
-  cudaFreeAsync(counts, stream);
+  cudaFreeAsync(L.order, stream);
+  cudaFreeAsync(L.pos, stream);
+  cudaFreeAsync(L.csize, stream);
+  cudaFreeAsync(L.diag, stream);
+  cudaFreeAsync(L.small, stream);
+  cudaFreeAsync(L.large, stream);
+  cudaFreeAsync(L.counters, stream);
   cudaFreeAsync(w_slot, stream);
-  cudaFreeAsync(v_slot, stream);
+  if (v_slot) cudaFreeAsync(v_slot, stream);
   cudaFreeAsync(Hh, stream);
   cudaFreeAsync(Sh, stream);
   cudaFreeAsync(h32, stream);
