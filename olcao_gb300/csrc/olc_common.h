@@ -244,4 +244,8 @@ int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, 
 int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
                   double* eigenvalues, int flags, double* vectors);
 
+// batched FP32 eigen-solve (olc_tridiag.cu)
+int hetrd_max_n();
+int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X);
+
 }  // namespace olc

@@ -5,8 +5,9 @@
 // 1 TFLOP/s while BF16 tensor-core products run above 1 PFLOP/s, so the
 // FP64-accurate answer is recovered from an FP32 solve instead:
 //
-//   1. FP32 pencil: cuSOLVER chegvd per k (concurrent streams) gives X (n x n,
-//      S-orthonormal to FP32 accuracy) and its eigenvalues.
+//   1. FP32 pencil: X (n x n, S-orthonormal to FP32 accuracy) from the
+//      batched FP32 solver of olc_tridiag.cu (all k in one set of launches),
+//      or from cuSOLVER chegvd per k on concurrent streams.
 //   2. Rayleigh-Ritz in that basis with FP64-accurate products:
 //        Hh = X^H (H X),  Sh = X^H (S X).
 //      Each product is formed error-free from BF16 slices on the tensor cores
@@ -32,6 +33,8 @@
 // so that a length-2k sum of products stays exact in FP32 (6 bits at k = 832).
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <cuda_bf16.h>
 
 #include "olc_common.h"
@@ -809,25 +812,15 @@ int loewdin(olc_context* ctx, int n, int nk, double* Hh, double* Sh, float* X) {
   return cuda_check(cudaGetLastError(), "loewdin kernels");
 }
 
-// Solve every k with the mixed-precision scheme; h, s are full Hermitian
-// FP64 [nk][n][n] (not modified).
-int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
-                     double* eig_dev, double* vectors) {
-  const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
-  if (n > kSortMax) return fail(OLC_ERR_UNSUPPORTED, "mixed solver: n above 8192");
+// FP32 eigenvectors by cuSOLVER chegvd, one k per call, the calls spread over
+// host threads and streams (chegvd waits on the device from its host thread).
+// X overwrites h32; s32 is overwritten.
+static int solve_fp32_library(olc_context* ctx, int n, int nk, float* h32, float* s32) {
   const size_t nn = (size_t)n * n;
-  int st;
   cudaStream_t stream = ctx->stream;
-  // ---- 1. FP32 generalised solve per k -----------------------------------
-  float *h32 = nullptr, *s32 = nullptr, *w32 = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
+  int st;
+  float* w32 = nullptr;
   if ((st = cuda_check(cudaMallocAsync((void**)&w32, 4 * (size_t)n * nk, stream), "malloc w32"))) return st;
-  {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 2);
-    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
-    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
-  }
   const int nsub = std::max(1, std::min(nk, 32));
   if ((int)ctx->mixed_streams.size() != nsub || ctx->mixed_n != n) {
     for (size_t i = 0; i < ctx->mixed_streams.size(); ++i) {
@@ -889,9 +882,46 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
       cudaStreamWaitEvent(stream, ctx->mixed_join[i], 0);
     }
   }
-  cudaFreeAsync(s32, stream);
   cudaFreeAsync(w32, stream);
-  float* X = h32;         // FP32 eigenvectors, [nk][n][n] complex
+  return OLC_OK;
+}
+
+// The batched FP32 solver is used unless OLC_FP32_SOLVER=library or n is
+// beyond its shared-memory limit.
+static bool use_batched_fp32(int n) {
+  const char* v = std::getenv("OLC_FP32_SOLVER");
+  if (v && std::string(v) == "library") return false;
+  return n >= 2 && n <= hetrd_max_n();
+}
+
+// Solve every k with the mixed-precision scheme; h, s are full Hermitian
+// FP64 [nk][n][n] (not modified).
+int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
+                     double* eig_dev, double* vectors) {
+  const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
+  if (n > kSortMax) return fail(OLC_ERR_UNSUPPORTED, "mixed solver: n above 8192");
+  const size_t nn = (size_t)n * n;
+  int st;
+  cudaStream_t stream = ctx->stream;
+  // ---- 1. FP32 generalised solve per k -----------------------------------
+  float *h32 = nullptr, *s32 = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 2);
+    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
+    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
+  }
+  float* X = nullptr;      // FP32 eigenvectors, [nk][n][n] complex
+  if (use_batched_fp32(n)) {
+    if ((st = cuda_check(cudaMallocAsync((void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
+    if ((st = solve_fp32_batched(ctx, n, nk, h32, s32, X))) return st;
+    cudaFreeAsync(h32, stream);
+  } else {
+    if ((st = solve_fp32_library(ctx, n, nk, h32, s32))) return st;
+    X = h32;
+  }
+  cudaFreeAsync(s32, stream);
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
   __nv_bfloat16 *wsA = nullptr, *wsB = nullptr;
   float* G = nullptr;
@@ -927,7 +957,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   // ---- 3. Loewdin transform: Sh = I + E  ->  (I+F)^H Hh (I+F), F = -E/2 + 3E^2/8
   // so that the pencil is standard; the products with the small F need only
   // FP32 (their relative error times |F| ~ 1e-5 is far below FP64 needs)
-  if ((st = loewdin(ctx, n, nk, Hh, Sh, h32))) return st;
+  if ((st = loewdin(ctx, n, nk, Hh, Sh, X))) return st;
   // ---- 4. clusters and their exact solves -----------------------------------
   ClusterLists L{};
   L.cap = (n / 2 + 1) * nk;
@@ -986,7 +1016,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   if (v_slot) cudaFreeAsync(v_slot, stream);
   cudaFreeAsync(Hh, stream);
   cudaFreeAsync(Sh, stream);
-  cudaFreeAsync(h32, stream);
+  cudaFreeAsync(X, stream);
   std::vector<int> hinfo(nk);
   cudaMemcpyAsync(hinfo.data(), ctx->d_info, sizeof(int) * nk, cudaMemcpyDeviceToHost, stream);
   int s2 = cuda_check(cudaStreamSynchronize(stream), "mixed solve sync");

@@ -1,0 +1,599 @@
+// Batched FP32 generalised Hermitian eigen-solve of every k at once: the FP32
+// stage of the mixed-precision solver (the role LAPACK chegv plays, restated
+// for one GPU and all k-points together).
+//
+//   1. S = U^H U (cuSOLVER potrfBatched) and C = U^{-H} H U^{-1} (two cuBLAS
+//      batched triangular solves).
+//   2. C = Q T Q^H by Householder reflectors H_i = I - tau_i v_i v_i^H, the
+//      lower-triangle reduction of LAPACK chetd2: one thread-block cluster per
+//      k owns the k's matrix in HBM, its CTAs own interleaved columns.  Every
+//      step i makes ONE pass over the trailing matrix that applies the pending
+//      rank-2 update of step i-1 (A -= v w^H + w v^H) and, in the same read,
+//      forms p = tau A v_i for step i.  The reflector vectors are broadcast and
+//      the products p exchanged through distributed shared memory; the cluster
+//      barrier orders the steps.
+//   3. T z = lambda z in FP64: eigenvalues by bisection on FP32 Sturm counts,
+//      eigenvectors by FP64 inverse iteration (LU with partial pivoting of
+//      T - sigma I, as LAPACK dstein), then modified Gram-Schmidt inside every
+//      group of eigenvalues too close for inverse iteration to separate.
+//   4. Back-transform Z = Q Z_T in blocks of 64 reflectors written as
+//      I - V T V^H (compact WY, LAPACK clarft), three strided-batched GEMMs
+//      per block.
+//   5. X = U^{-1} Z (cuBLAS batched triangular solve).
+// X is S-orthonormal and diagonalises H to FP32 accuracy; the Rayleigh-Ritz
+// step of the mixed solver takes it from there.
+#include <algorithm>
+#include <cfloat>
+#include <cooperative_groups.h>
+#include <cstdio>
+#include <vector>
+
+#include "olc_common.h"
+
+namespace cg = cooperative_groups;
+
+namespace olc {
+
+namespace {
+
+constexpr int kTrdThreads = 512;
+constexpr int kWyBlock = 64;         // reflectors per compact-WY block
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// Sum over the CTA in FP64 (red: >= 33 doubles of shared memory).
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// ---------------------------------------------------------------------------
+// 2. Householder tridiagonalisation, one cluster of G CTAs per k
+// ---------------------------------------------------------------------------
+// A: [nk][n][n] complex FP32, column-major, full Hermitian.  On return
+// column i holds v_i in rows i+1..n-1 (v_i(i+1) = 1), d[k][i] the diagonal of
+// T, e[k][i] its (real) off-diagonal, tau[k][i] the reflector factors.
+// Column r belongs to CTA r % G of the cluster for the whole reduction, so
+// only the cluster's shared memory crosses CTAs.
+__global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__ A, int n,
+                                                            double* __restrict__ dout,
+                                                            double* __restrict__ eout,
+                                                            float2* __restrict__ tout) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int G = (int)cl.num_blocks();
+  const int rank = (int)cl.block_rank();
+  const int k = blockIdx.y;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  float2* Ak = A + (size_t)k * n * n;
+  extern __shared__ float2 trd_sm[];
+  __shared__ double red[40];
+  __shared__ float2 s_tau, s_scale;
+  int cur = 0;
+  bool pend = false;
+  for (int i = 0; i < n - 1; ++i) {
+    float2* vC = trd_sm + (size_t)(2 * cur) * n;       // v_i
+    float2* wC = trd_sm + (size_t)(2 * cur + 1) * n;   // p_i, then w_i
+    const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;      // pending v_{i-1}
+    const float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;  // pending w_{i-1}
+    // ---- (a) owner of column i: pending update, reflector of column i ------
+    if (rank == i % G) {
+      float2* col = Ak + (size_t)i * n;
+      float2 cw = make_float2(0.f, 0.f), cv = cw;
+      if (pend) { cw = conjf2(wP[i]); cv = conjf2(vP[i]); }
+      double part = 0.0;
+      for (int r = i + tid; r < n; r += blockDim.x) {
+        float2 a = col[r];
+        if (pend) {
+          const float2 t1 = cmul(vP[r], cw), t2 = cmul(wP[r], cv);
+          a.x -= t1.x + t2.x;
+          a.y -= t1.y + t2.y;
+        }
+        if (r == i) dout[(size_t)k * n + i] = a.x;
+        else vC[r] = a;
+        if (r >= i + 2) part += (double)a.x * a.x + (double)a.y * a.y;
+      }
+      const double xn2 = block_sum_d(part, red);
+      if (tid == 0) {
+        const float2 al = vC[i + 1];
+        float2 tau = make_float2(0.f, 0.f), scale = make_float2(0.f, 0.f);
+        double beta = al.x;
+        if (!(xn2 == 0.0 && al.y == 0.f)) {
+          const double an = sqrt((double)al.x * al.x + (double)al.y * al.y + xn2);
+          beta = (al.x >= 0.f) ? -an : an;
+          tau = make_float2((float)((beta - al.x) / beta), (float)(-al.y / beta));
+          const double dr = al.x - beta, di = al.y, den = dr * dr + di * di;
+          scale = make_float2((float)(dr / den), (float)(-di / den));
+        }
+        eout[(size_t)k * (n - 1) + i] = beta;
+        tout[(size_t)k * (n - 1) + i] = tau;
+        s_tau = tau;
+        s_scale = scale;
+        for (int g = 0; g < G; ++g)
+          if (g != rank) *cl.map_shared_rank(&s_tau, g) = tau;
+      }
+      __syncthreads();
+      const float2 scale = s_scale;
+      for (int r = i + 1 + tid; r < n; r += blockDim.x) {
+        const float2 v = (r == i + 1) ? make_float2(1.f, 0.f) : cmul(vC[r], scale);
+        vC[r] = v;
+        col[r] = v;
+        for (int g = 0; g < G; ++g)
+          if (g != rank) cl.map_shared_rank(vC, g)[r] = v;
+      }
+    }
+    cl.sync();
+    // ---- (b) one pass over the owned trailing columns ----------------------
+    const float2 tau = s_tau;
+    int r0 = i + 1;
+    r0 += ((rank - r0) % G + G) % G;
+    for (int r = r0 + warp * G; r < n; r += nwarps * G) {
+      float2* col = Ak + (size_t)r * n;
+      float2 cw = make_float2(0.f, 0.f), cv = cw;
+      if (pend) { cw = conjf2(wP[r]); cv = conjf2(vP[r]); }
+      float ax = 0.f, ay = 0.f;
+      int c = i + 1 + lane;
+      for (; c + 96 < n; c += 128) {
+        float2 a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] = col[c + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int cc = c + 32 * u;
+          if (pend) {
+            const float2 t1 = cmul(vP[cc], cw), t2 = cmul(wP[cc], cv);
+            a[u].x -= t1.x + t2.x;
+            a[u].y -= t1.y + t2.y;
+            col[cc] = a[u];
+          }
+          const float2 v = vC[cc];
+          ax += a[u].x * v.x + a[u].y * v.y;       // conj(a) v
+          ay += a[u].x * v.y - a[u].y * v.x;
+        }
+      }
+      for (; c < n; c += 32) {
+        float2 a = col[c];
+        if (pend) {
+          const float2 t1 = cmul(vP[c], cw), t2 = cmul(wP[c], cv);
+          a.x -= t1.x + t2.x;
+          a.y -= t1.y + t2.y;
+          col[c] = a;
+        }
+        const float2 v = vC[c];
+        ax += a.x * v.x + a.y * v.y;
+        ay += a.x * v.y - a.y * v.x;
+      }
+      for (int o = 16; o; o >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+      }
+      if (lane == 0) {
+        const float2 p = cmul(tau, make_float2(ax, ay));
+        for (int g = 0; g < G; ++g) cl.map_shared_rank(wC, g)[r] = p;
+      }
+    }
+    cl.sync();
+    // ---- (c) w_i = p + alpha v, alpha = -tau/2 (p^H v) ----------------------
+    double sx = 0.0, sy = 0.0;
+    for (int c = i + 1 + tid; c < n; c += blockDim.x) {
+      const float2 p = wC[c], v = vC[c];
+      sx += (double)p.x * v.x + (double)p.y * v.y;
+      sy += (double)p.x * v.y - (double)p.y * v.x;
+    }
+    sx = block_sum_d(sx, red);
+    sy = block_sum_d(sy, red);
+    const float2 al2 = make_float2((float)(-0.5 * (tau.x * sx - tau.y * sy)),
+                                   (float)(-0.5 * (tau.x * sy + tau.y * sx)));
+    for (int c = i + 1 + tid; c < n; c += blockDim.x) {
+      const float2 t = cmul(al2, vC[c]);
+      wC[c].x += t.x;
+      wC[c].y += t.y;
+    }
+    __syncthreads();
+    pend = true;
+    cur ^= 1;
+  }
+  // last diagonal element after the final pending update
+  const int last = n - 1;
+  if (rank == last % G && tid == 0) {
+    float2 a = Ak[(size_t)last * n + last];
+    if (pend) {
+      const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;
+      const float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;
+      const float2 t1 = cmul(vP[last], conjf2(wP[last])), t2 = cmul(wP[last], conjf2(vP[last]));
+      a.x -= t1.x + t2.x;
+    }
+    dout[(size_t)k * n + last] = a.x;
+  }
+  cl.sync();
+}
+
+// ---------------------------------------------------------------------------
+// 3. tridiagonal eigen-solve
+// ---------------------------------------------------------------------------
+// Eigenvalue j (ascending) of T_k by bisection on Sturm counts (FP32): the
+// count of eigenvalues below x is the number of negative pivots of the LDL^T
+// factorisation of T - x I (q_i = d_i - x - e_{i-1}^2 / q_{i-1}, pivots below
+// pivmin replaced by -pivmin as in LAPACK dstebz).
+__global__ void bisect_kernel(const double* __restrict__ d, const double* __restrict__ e, int n,
+                              int nk, double* __restrict__ lam) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * nk) return;
+  const int k = t / n, j = t % n;
+  const double* dk = d + (size_t)k * n;
+  const double* ek = e + (size_t)k * (n - 1);
+  float lo = FLT_MAX, hi = -FLT_MAX, emax2 = 0.f;
+  for (int i = 0; i < n; ++i) {
+    const float el = i > 0 ? fabsf((float)ek[i - 1]) : 0.f, er = i < n - 1 ? fabsf((float)ek[i]) : 0.f;
+    const float di = (float)dk[i];
+    lo = fminf(lo, di - el - er);
+    hi = fmaxf(hi, di + el + er);
+    emax2 = fmaxf(emax2, er * er);
+  }
+  const float pivmin = 1e-30f * fmaxf(1.f, emax2);
+  const float w = fmaxf(fabsf(lo), fabsf(hi));
+  lo -= 4e-6f * w + 2.f * pivmin;
+  hi += 4e-6f * w + 2.f * pivmin;
+  for (int it = 0; it < 80; ++it) {
+    const float mid = 0.5f * (lo + hi);
+    if (hi - lo <= 2.f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)) + pivmin || mid == lo || mid == hi) break;
+    int cnt = 0;
+    float q = (float)dk[0] - mid;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    cnt += q < 0.f;
+    for (int i = 1; i < n; ++i) {
+      const float ei = (float)ek[i - 1];
+      q = (float)dk[i] - mid - ei * ei / q;
+      if (fabsf(q) < pivmin) q = -pivmin;
+      cnt += q < 0.f;
+    }
+    if (cnt > j) hi = mid; else lo = mid;
+  }
+  lam[t] = 0.5 * ((double)lo + (double)hi);
+}
+
+// Inverse iteration in FP64 for eigenvalue j of T_k (one thread each):
+// T - sigma I = P L U with partial pivoting (U has two super-diagonals), tiny
+// pivots replaced by eps * ||T||, three solves from a pseudo-random start.
+// Work arrays are interleaved ([i][thread]) so that a warp's accesses
+// coalesce.  Z: [nk][n][n] FP64, column j = eigenvector j.
+__global__ void invit_kernel(const double* __restrict__ d, const double* __restrict__ e,
+                             const double* __restrict__ lam, int n, int nk,
+                             double* __restrict__ work, unsigned char* __restrict__ piv,
+                             double* __restrict__ Z) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int T = n * nk;
+  if (t >= T) return;
+  const int k = t / n, j = t % n;
+  const double* dk = d + (size_t)k * n;
+  const double* ek = e + (size_t)k * (n - 1);
+  double* Lm = work;                      // multipliers
+  double* U0 = work + (size_t)n * T;      // 1 / diagonal of U
+  double* U1 = work + (size_t)2 * n * T;  // first super-diagonal
+  double* U2 = work + (size_t)3 * n * T;  // second super-diagonal
+  double* x = work + (size_t)4 * n * T;   // iterate
+  const double sigma = lam[t];
+  double tn = 0.0;
+  for (int i = 0; i < n; ++i) tn = fmax(tn, fabs(dk[i]) + (i > 0 ? fabs(ek[i - 1]) : 0.0) + (i < n - 1 ? fabs(ek[i]) : 0.0));
+  const double tiny = 2.2e-16 * fmax(tn, 1e-300);
+  // factorisation
+  double a = dk[0] - sigma, b = n > 1 ? ek[0] : 0.0;
+  for (int i = 0; i < n - 1; ++i) {
+    const double sub = ek[i], nd = dk[i + 1] - sigma, ns = (i + 1 < n - 1) ? ek[i + 1] : 0.0;
+    const size_t o = (size_t)i * T + t;
+    if (fabs(a) >= fabs(sub)) {
+      if (fabs(a) < tiny) a = a >= 0.0 ? tiny : -tiny;
+      const double m = sub / a;
+      U0[o] = 1.0 / a; U1[o] = b; U2[o] = 0.0; Lm[o] = m; piv[o] = 0;
+      a = nd - m * b;
+      b = ns;
+    } else {
+      const double m = a / sub;
+      U0[o] = 1.0 / sub; U1[o] = nd; U2[o] = ns; Lm[o] = m; piv[o] = 1;
+      a = b - m * nd;
+      b = -m * ns;
+    }
+  }
+  if (fabs(a) < tiny) a = a >= 0.0 ? tiny : -tiny;
+  U0[(size_t)(n - 1) * T + t] = 1.0 / a;
+  // start vector: a fixed pseudo-random sequence per (j, i)
+  unsigned s = 0x9e3779b9u * (unsigned)(j + 1) ^ 0x85ebca6bu;
+  for (int i = 0; i < n; ++i) {
+    s ^= s << 13; s ^= s >> 17; s ^= s << 5;
+    x[(size_t)i * T + t] = (double)(s & 0xffffff) / 16777216.0 - 0.5;
+  }
+  for (int it = 0; it < 3; ++it) {
+    // forward: apply P and L
+    for (int i = 0; i < n - 1; ++i) {
+      const size_t o = (size_t)i * T + t, o1 = o + T;
+      double yi = x[o], yn = x[o1];
+      if (piv[o]) { const double tmp = yi; yi = yn; yn = tmp; x[o] = yi; }
+      x[o1] = yn - Lm[o] * yi;
+    }
+    // back substitution with U, scaled to max |x| = 1
+    double x1 = 0.0, x2 = 0.0, amax = 0.0;
+    for (int i = n - 1; i >= 0; --i) {
+      const size_t o = (size_t)i * T + t;
+      const double xi = (x[o] - U1[o] * x1 - U2[o] * x2) * U0[o];
+      x[o] = xi;
+      x2 = x1;
+      x1 = xi;
+      amax = fmax(amax, fabs(xi));
+    }
+    const double sc = amax > 0.0 ? 1.0 / amax : 1.0;
+    for (int i = 0; i < n; ++i) x[(size_t)i * T + t] *= sc;
+  }
+  double nrm = 0.0;
+  for (int i = 0; i < n; ++i) { const double v = x[(size_t)i * T + t]; nrm += v * v; }
+  const double sc = 1.0 / sqrt(nrm);
+  double* z = Z + ((size_t)k * n + j) * n;
+  for (int i = 0; i < n; ++i) z[i] = x[(size_t)i * T + t] * sc;
+}
+
+// Modified Gram-Schmidt (twice) inside every group of consecutive
+// eigenvalues closer than tol * max|lambda|: inverse iteration cannot separate
+// those, any orthonormal basis of their span serves.  One CTA per k; thread 0
+// lists the groups, one warp per group.  Writes the result as complex FP32
+// columns into Zc [nk][n][n].
+__global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict__ lam,
+                                                        double* __restrict__ Z, int n, double tol,
+                                                        float2* __restrict__ Zc) {
+  extern __shared__ int gstart[];
+  __shared__ int ng;
+  const int k = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const double* lk = lam + (size_t)k * n;
+  if (tid == 0) {
+    double amax = 0.0;
+    for (int j = 0; j < n; ++j) amax = fmax(amax, fabs(lk[j]));
+    const double thr = tol * fmax(amax, 1e-300);
+    int c = 0, s0 = 0;
+    for (int j = 1; j <= n; ++j) {
+      if (j == n || lk[j] - lk[j - 1] > thr) {
+        if (j - s0 > 1) { gstart[2 * c] = s0; gstart[2 * c + 1] = j; ++c; }
+        s0 = j;
+      }
+    }
+    ng = c;
+  }
+  __syncthreads();
+  double* Zk = Z + (size_t)k * n * n;
+  for (int g = warp; g < ng; g += blockDim.x >> 5) {
+    const int s0 = gstart[2 * g], s1 = gstart[2 * g + 1];
+    for (int m = s0 + 1; m < s1; ++m) {
+      double* zm = Zk + (size_t)m * n;
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int q = s0; q < m; ++q) {
+          const double* zq = Zk + (size_t)q * n;
+          double dt = 0.0;
+          for (int i = lane; i < n; i += 32) dt += zq[i] * zm[i];
+          for (int o = 16; o; o >>= 1) dt += __shfl_xor_sync(0xffffffffu, dt, o);
+          for (int i = lane; i < n; i += 32) zm[i] -= dt * zq[i];
+          __syncwarp();
+        }
+        double nr = 0.0;
+        for (int i = lane; i < n; i += 32) nr += zm[i] * zm[i];
+        for (int o = 16; o; o >>= 1) nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        const double sc = nr > 0.0 ? 1.0 / sqrt(nr) : 0.0;
+        for (int i = lane; i < n; i += 32) zm[i] *= sc;
+        __syncwarp();
+      }
+    }
+  }
+  __syncthreads();
+  float2* Zck = Zc + (size_t)k * n * n;
+  for (size_t e = tid; e < (size_t)n * n; e += blockDim.x) Zck[e] = make_float2((float)Zk[e], 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// 4. compact-WY back-transform
+// ---------------------------------------------------------------------------
+// V block: reflectors j0..j0+nb-1 on rows j0+1..n-1 (L rows), zero above each
+// reflector's leading 1.  V: [nk][nb][L] complex, column-major.
+__global__ void build_v_kernel(const float2* __restrict__ A, int n, int j0, int nb, int L,
+                               int nk, float2* __restrict__ V) {
+  const size_t total = (size_t)nk * nb * L;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int rr = (int)(e % L);
+    const int tcol = (int)((e / L) % nb);
+    const int k = (int)(e / ((size_t)L * nb));
+    const int r = j0 + 1 + rr, j = j0 + tcol;
+    V[e] = (r >= j + 1) ? A[(size_t)k * n * n + (size_t)j * n + r] : make_float2(0.f, 0.f);
+  }
+}
+
+// T factor of the block (LAPACK clarft, forward, columnwise), one CTA per k:
+// T(s,s) = tau_s, T(s,t) = -tau_t sum_{u=s}^{t-1} T(s,u) (V^H V)(u,t); thread s
+// owns row s.  Gm: [nk][nb][nb] = V^H V; Tm: [nk][nb][nb] column-major.
+__global__ void tfactor_kernel(const float2* __restrict__ Gm, const float2* __restrict__ tau, int n,
+                               int j0, int nb, float2* __restrict__ Tm) {
+  const int k = blockIdx.x, s = threadIdx.x;
+  if (s >= nb) return;
+  const float2* G = Gm + (size_t)k * nb * nb;
+  const float2* tk = tau + (size_t)k * (n - 1) + j0;
+  float2* T = Tm + (size_t)k * nb * nb;
+  for (int t = 0; t < nb; ++t) {
+    float2 v = make_float2(0.f, 0.f);
+    if (t == s) {
+      v = tk[s];
+    } else if (t > s) {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int u = s; u < t; ++u) {
+        const float2 p = cmul(T[(size_t)u * nb + s], G[(size_t)t * nb + u]);
+        acc.x += p.x;
+        acc.y += p.y;
+      }
+      const float2 q = cmul(tk[t], acc);
+      v = make_float2(-q.x, -q.y);
+    }
+    T[(size_t)t * nb + s] = v;
+  }
+}
+
+__global__ void ptr_array_kernel(float2* base, size_t stride, int nk, float2** out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nk) out[k] = base + (size_t)k * stride;
+}
+
+}  // namespace
+
+int hetrd_max_n() {
+  int dev = 0, smem = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return (smem - 2048) / (4 * (int)sizeof(float2));
+}
+
+// FP32 eigenvectors X (S-orthonormal, [nk][n][n] complex column-major) of
+// every pencil (h32, s32).  h32 and s32 are overwritten (reduced matrix and
+// reflectors; Cholesky factor).  ctx->d_info receives potrf's info per k.
+int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X) {
+  cudaStream_t stream = ctx->stream;
+  const size_t nn = (size_t)n * n;
+  int st;
+  if (n < 2) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver needs n >= 2");
+  if (n > hetrd_max_n()) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver: n above the shared-memory limit");
+  auto* H = reinterpret_cast<float2*>(h32);
+  auto* Sm = reinterpret_cast<float2*>(s32);
+  auto* Xc = reinterpret_cast<float2*>(X);
+  float2** ptrs = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&ptrs, sizeof(float2*) * 3 * nk, stream), "malloc ptrs"))) return st;
+  ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Sm, nn, nk, ptrs);
+  ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(H, nn, nk, ptrs + nk);
+  ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Xc, nn, nk, ptrs + 2 * nk);
+  const cuComplex one = make_cuComplex(1.f, 0.f), mone = make_cuComplex(-1.f, 0.f),
+                  zero = make_cuComplex(0.f, 0.f);
+  auto** Sp = reinterpret_cast<cuComplex**>(ptrs);
+  auto** Hp = reinterpret_cast<cuComplex**>(ptrs + nk);
+  auto** Xp = reinterpret_cast<cuComplex**>(ptrs + 2 * nk);
+  // ---- 1. Cholesky and reduction ------------------------------------------
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
+    cusolverDnSetStream(ctx->solver, stream);
+    if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
+    if (cusolverDnCpotrfBatched(ctx->solver, CUBLAS_FILL_MODE_UPPER, n, Sp, n, ctx->d_info, nk) !=
+        CUSOLVER_STATUS_SUCCESS)
+      return fail(OLC_ERR_CUDA, "cusolverDnCpotrfBatched failed");
+    if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C,
+                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, n, Hp, n, nk) != CUBLAS_STATUS_SUCCESS)
+      return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-H H) failed");
+    if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, n, Hp, n, nk) != CUBLAS_STATUS_SUCCESS)
+      return fail(OLC_ERR_CUDA, "ctrsmBatched (H U^-1) failed");
+  }
+  // ---- 2. tridiagonalisation ----------------------------------------------
+  double *d = nullptr, *e = nullptr, *lam = nullptr, *work = nullptr, *Z = nullptr;
+  float2* tau = nullptr;
+  unsigned char* piv = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&d, 8ULL * n * nk, stream), "malloc d"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&e, 8ULL * (n - 1) * nk, stream), "malloc e"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 1);
+    int G = 1;
+    while (G < 8 && (G * 2) * nk <= 152) G *= 2;
+    const size_t smem = 4 * sizeof(float2) * (size_t)n;
+    if ((st = cuda_check(cudaFuncSetAttribute(hetrd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem), "hetrd smem"))) return st;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(G, nk, 1);
+    cfg.blockDim = dim3(kTrdThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if ((st = cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel, H, n, d, e, tau), "hetrd launch"))) return st;
+  }
+  // ---- 3. tridiagonal eigen-solve -------------------------------------------
+  const size_t T = (size_t)n * nk;
+  if ((st = cuda_check(cudaMallocAsync((void**)&lam, 8ULL * T, stream), "malloc lam"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&work, 8ULL * 5 * n * T, stream), "malloc invit work"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&piv, (size_t)n * T, stream), "malloc piv"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&Z, 8ULL * nn * nk, stream), "malloc Z"))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
+    bisect_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(d, e, n, nk, lam);
+    invit_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(d, e, lam, n, nk, work, piv, Z);
+    const size_t gsm = sizeof(int) * 2 * (size_t)(n / 2 + 1);
+    if ((st = cuda_check(cudaFuncSetAttribute(group_mgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)gsm), "mgs smem"))) return st;
+    group_mgs_kernel<<<nk, 256, gsm, stream>>>(lam, Z, n, 1e-5, Xc);
+  }
+  cudaFreeAsync(work, stream);
+  cudaFreeAsync(piv, stream);
+  // ---- 4. back-transform X = Q Z_T ------------------------------------------
+  {
+    const int nblk = (n - 1 + kWyBlock - 1) / kWyBlock;
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
+    float2 *V = nullptr, *Gm = nullptr, *Tm = nullptr, *W1 = nullptr, *W2 = nullptr;
+    const size_t nb = kWyBlock;
+    if ((st = cuda_check(cudaMallocAsync((void**)&V, 8ULL * nb * n * nk, stream), "malloc V"))) return st;
+    if ((st = cuda_check(cudaMallocAsync((void**)&Gm, 8ULL * nb * nb * nk, stream), "malloc G"))) return st;
+    if ((st = cuda_check(cudaMallocAsync((void**)&Tm, 8ULL * nb * nb * nk, stream), "malloc T"))) return st;
+    if ((st = cuda_check(cudaMallocAsync((void**)&W1, 8ULL * nb * n * nk, stream), "malloc W1"))) return st;
+    if ((st = cuda_check(cudaMallocAsync((void**)&W2, 8ULL * nb * n * nk, stream), "malloc W2"))) return st;
+    auto* Vc = reinterpret_cast<cuComplex*>(V);
+    auto* Gc = reinterpret_cast<cuComplex*>(Gm);
+    auto* Tc = reinterpret_cast<cuComplex*>(Tm);
+    auto* W1c = reinterpret_cast<cuComplex*>(W1);
+    auto* W2c = reinterpret_cast<cuComplex*>(W2);
+    auto* Zx = reinterpret_cast<cuComplex*>(Xc);
+    for (int b = nblk - 1; b >= 0; --b) {
+      const int j0 = b * kWyBlock;
+      const int nbb = std::min(kWyBlock, n - 1 - j0);
+      const int L = n - j0 - 1;
+      const long long sV = (long long)nbb * L, sG = (long long)nbb * nbb, sW = (long long)nbb * n;
+      build_v_kernel<<<std::min<size_t>((sV * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, j0, nbb, L, nk, V);
+      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
+                                    &zero, Gc, nbb, sG, nk) != CUBLAS_STATUS_SUCCESS)
+        return fail(OLC_ERR_CUDA, "cgemm V^H V failed");
+      tfactor_kernel<<<nk, 64, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
+      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
+                                    Zx + j0 + 1, n, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
+        return fail(OLC_ERR_CUDA, "cgemm V^H Z failed");
+      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, nbb, n, nbb, &one, Tc, nbb, sG,
+                                    W1c, nbb, sW, &zero, W2c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
+        return fail(OLC_ERR_CUDA, "cgemm T W failed");
+      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, L, n, nbb, &mone, Vc, L, sV,
+                                    W2c, nbb, sW, &one, Zx + j0 + 1, n, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
+        return fail(OLC_ERR_CUDA, "cgemm Z -= V W failed");
+      scope.add_launches(2);
+    }
+    cudaFreeAsync(V, stream);
+    cudaFreeAsync(Gm, stream);
+    cudaFreeAsync(Tm, stream);
+    cudaFreeAsync(W1, stream);
+    cudaFreeAsync(W2, stream);
+  }
+  // ---- 5. X = U^{-1} Z --------------------------------------------------------
+  {
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
+    if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, n, Xp, n, nk) != CUBLAS_STATUS_SUCCESS)
+      return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-1 Z) failed");
+  }
+  cudaFreeAsync(d, stream);
+  cudaFreeAsync(e, stream);
+  cudaFreeAsync(tau, stream);
+  cudaFreeAsync(lam, stream);
+  cudaFreeAsync(Z, stream);
+  cudaFreeAsync(ptrs, stream);
+  return cuda_check(cudaGetLastError(), "batched FP32 solve");
+}
+
+}  // namespace olc
