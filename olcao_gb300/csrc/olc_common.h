@@ -244,6 +244,15 @@ int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, 
 int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
                   double* eigenvalues, int flags, double* vectors);
 
+// FP64-accurate complex products from BF16 tensor-core digits (olc_ozaki.cu):
+// C[b] = op(A[b]) B[b], A logical m x k (conjA: A = src^H), B k x n, C m x n
+// complex FP64 with batch stride m*n; bits_a/bits_b = bits kept per operand.
+template <class TA, class TB>
+int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
+                bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
+                int nb);
+void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
+
 // batched FP32 eigen-solve (olc_tridiag.cu)
 int hetrd_max_n();
 int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X);

@@ -9,15 +9,9 @@
 //      batched FP32 solver of olc_tridiag.cu (all k in one set of launches),
 //      or from cuSOLVER chegvd per k on concurrent streams.
 //   2. Rayleigh-Ritz in that basis with FP64-accurate products:
-//        Hh = X^H (H X),  Sh = X^H (S X).
-//      Each product is formed error-free from BF16 slices on the tensor cores
-//      (the splitting of Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59
-//      (2012) 95-118): every row (left operand) or column (right operand) is
-//      scaled by a power of two and cut into short integer slices, which BF16
-//      holds exactly; every slice product accumulates integers below 2^24 in
-//      FP32, hence exactly; the slice products are summed with their scales
-//      in FP64.  Complex products use the real embedding
-//      [[Ar,-Ai],[Ai,Ar]] [[Br],[Bi]].
+//        Hh = X^H (H X),  Sh = X^H (S X),
+//      each formed error-free from BF16 digits on the tensor cores
+//      (olc_ozaki.cu).
 //   3. Sh = I + E with E ~ 1e-5: the Loewdin transform (I+F)^H Hh (I+F),
 //      F = -E/2 + 3E^2/8, makes the pencil standard to O(E^3); since F is
 //      small its products need only FP32 GEMMs.  The basis becomes X (I+F).
@@ -29,8 +23,6 @@
 //      cluster is diagonalised by an FP32 Jacobi solver after the shift by
 //      its mean energy (the shifted block's norm is the cluster width, so
 //      FP32 rounding stays near 1e-8 Ha).  Eigenvectors are X z.
-// The slices hold ceil(bits / beta) integer chunks per operand, beta chosen
-// so that a length-2k sum of products stays exact in FP32 (6 bits at k = 832).
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -58,156 +50,10 @@ __global__ void to_c64_kernel(const double* __restrict__ in, float* __restrict__
     out[i] = (float)in[i];
 }
 
-// ---------------------------------------------------------------------------
-// error-free slicing
-// ---------------------------------------------------------------------------
-// Logical complex operand: element (r, c) of an (rows x cols) matrix, read
-// from a column-major source with leading dimension ld.  conj_trans reads the
-// conjugate transpose of the source.
-template <class T>
-__device__ __forceinline__ void load_c(const T* src, int ld, bool conj_trans, int r, int c,
-                                       double& re, double& im) {
-  if (!conj_trans) {
-    re = (double)src[2 * ((size_t)c * ld + r)];
-    im = (double)src[2 * ((size_t)c * ld + r) + 1];
-  } else {
-    re = (double)src[2 * ((size_t)r * ld + c)];
-    im = -(double)src[2 * ((size_t)r * ld + c) + 1];
-  }
-}
-
-// exponent e with max|x| < 2^e over a row (left operand) or column (right)
-template <class T>
-__global__ void exponent_kernel(const T* __restrict__ src, long long src_stride, int ld,
-                                bool conj_trans, int rows, int cols, bool per_row,
-                                int* __restrict__ expo, int nb) {
-  const int lines = per_row ? rows : cols;
-  const int len = per_row ? cols : rows;
-  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gwarp >= lines * nb) return;
-  const int b = gwarp / lines, line = gwarp % lines;
-  const T* s = src + (size_t)b * src_stride;
-  double mx = 0.0;
-  for (int t = lane; t < len; t += 32) {
-    double re, im;
-    if (per_row) load_c(s, ld, conj_trans, line, t, re, im);
-    else load_c(s, ld, conj_trans, t, line, re, im);
-    mx = fmax(mx, fmax(fabs(re), fabs(im)));
-  }
-  for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0) {
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);      // mx = f 2^e, f in [0.5, 1): |x| < 2^e
-    else e = -1000;
-    expo[(size_t)b * lines + line] = e;
-  }
-}
-
-// Left operand (m x k complex) -> nsl slices of the real embedding
-// (2m x 2k, column-major) as BF16 integers; per-row exponents.
-template <class T>
-__global__ void slice_left_kernel(const T* __restrict__ src, long long src_stride, int ld,
-                                  bool conj_trans, int m, int k, const int* __restrict__ expo,
-                                  int nsl, int beta, __nv_bfloat16* __restrict__ out, int nb) {
-  const size_t per = (size_t)m * k;
-  const size_t total = per * nb;
-  const size_t big = (size_t)4 * m * k;   // one slice of one batch entry
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (size_t)gridDim.x * blockDim.x) {
-    const int b = (int)(idx / per);
-    const size_t q = idx % per;
-    const int r = (int)(q % m), c = (int)(q / m);
-    double re, im;
-    load_c(src + (size_t)b * src_stride, ld, conj_trans, r, c, re, im);
-    const int e = expo[(size_t)b * m + r];
-    double ar = ldexp(re, -e), ai = ldexp(im, -e);
-    __nv_bfloat16* o = out + (size_t)b * nsl * big;
-    const size_t M2 = 2 * (size_t)m;
-    for (int s = 0; s < nsl; ++s) {
-      const double tr = ldexp(ar, beta), ti = ldexp(ai, beta);
-      const double qr = trunc(tr), qi = trunc(ti);
-      ar = tr - qr;
-      ai = ti - qi;
-      __nv_bfloat16* os = o + (size_t)s * big;
-      const __nv_bfloat16 br = __float2bfloat16_rn((float)qr);
-      const __nv_bfloat16 bi = __float2bfloat16_rn((float)qi);
-      const __nv_bfloat16 nbi = __float2bfloat16_rn((float)-qi);
-      os[(size_t)c * M2 + r] = br;                        // [r, c]     = Ar
-      os[(size_t)(c + k) * M2 + r] = nbi;                 // [r, c+k]   = -Ai
-      os[(size_t)c * M2 + r + m] = bi;                    // [r+m, c]   = Ai
-      os[(size_t)(c + k) * M2 + r + m] = br;              // [r+m, c+k] = Ar
-    }
-  }
-}
-
-// Right operand (k x n complex) -> nsl slices of [[Br],[Bi]] (2k x n); per-column exponents.
-template <class T>
-__global__ void slice_right_kernel(const T* __restrict__ src, long long src_stride, int ld,
-                                   int k, int n, const int* __restrict__ expo, int nsl, int beta,
-                                   __nv_bfloat16* __restrict__ out, int nb) {
-  const size_t per = (size_t)k * n;
-  const size_t total = per * nb;
-  const size_t big = (size_t)2 * k * n;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (size_t)gridDim.x * blockDim.x) {
-    const int b = (int)(idx / per);
-    const size_t q = idx % per;
-    const int r = (int)(q % k), c = (int)(q / k);
-    double re, im;
-    load_c(src + (size_t)b * src_stride, ld, false, r, c, re, im);
-    const int e = expo[(size_t)b * n + c];
-    double ar = ldexp(re, -e), ai = ldexp(im, -e);
-    __nv_bfloat16* o = out + (size_t)b * nsl * big;
-    const size_t K2 = 2 * (size_t)k;
-    for (int s = 0; s < nsl; ++s) {
-      const double tr = ldexp(ar, beta), ti = ldexp(ai, beta);
-      const double qr = trunc(tr), qi = trunc(ti);
-      ar = tr - qr;
-      ai = ti - qi;
-      __nv_bfloat16* os = o + (size_t)s * big;
-      os[(size_t)c * K2 + r] = __float2bfloat16_rn((float)qr);
-      os[(size_t)c * K2 + r + k] = __float2bfloat16_rn((float)qi);
-    }
-  }
-}
-
-// C (m x n complex, FP64) (+)= 2^(e_r + f_c - shift) * G, G = [[Gr],[Gi]] (2m x n FP32);
-// blockIdx.y is the batch entry.
-__global__ void ozaki_accumulate_kernel(const float* __restrict__ G, const int* __restrict__ ea,
-                                        const int* __restrict__ fb, int m, int n, int shift,
-                                        bool first, double* __restrict__ C) {
-  const int b = blockIdx.y;
-  const int per = m * n;
-  const float* g = G + (size_t)b * 2 * per;
-  const int* e = ea + (size_t)b * m;
-  const int* f = fb + (size_t)b * n;
-  double* o = C + 2 * (size_t)b * per;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < per; q += gridDim.x * blockDim.x) {
-    const int r = q % m, c = q / m;
-    const double sc = ldexp(1.0, e[r] + f[c] - shift);
-    const double vr = (double)g[(size_t)c * 2 * m + r] * sc;
-    const double vi = (double)g[(size_t)c * 2 * m + r + m] * sc;
-    if (first) {
-      o[2 * (size_t)q] = vr;
-      o[2 * (size_t)q + 1] = vi;
-    } else {
-      o[2 * (size_t)q] += vr;
-      o[2 * (size_t)q + 1] += vi;
-    }
-  }
-}
-
 int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32); }
 
 // Bits per slice so that a length-2k sum of slice products stays below 2^24
 // (exact in FP32): 2 beta + ceil(log2(2k)) <= 24.
-int slice_bits(int k) {
-  int lg = 0;
-  while ((1LL << lg) < 2LL * k) ++lg;
-  return std::max(1, std::min(7, (24 - lg) / 2));
-}
-int max_slices(int bits, int k) { return (bits + slice_bits(k) - 1) / slice_bits(k); }
 
 // ---------------------------------------------------------------------------
 // extraction
@@ -660,60 +506,6 @@ __global__ void __launch_bounds__(1024) final_sort_kernel(const double* __restri
 
 }  // namespace
 
-// Error-free complex product C = op(A) B for a batch (see the file comment).
-// A: logical m x k (source column-major, ld lda, conj_trans reads A^H),
-// B: k x n (ld ldb).  T = double or float sources; na/nbs slices per operand.
-template <class TA, class TB>
-int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
-                bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
-                int nb, __nv_bfloat16* wsA, __nv_bfloat16* wsB, float* G, int* ea, int* fb) {
-  cudaStream_t st = ctx->stream;
-  StageScope scope(ctx, OLC_STAGE_REFINE, 0);
-  const int beta = slice_bits(k);
-  const int na = (bits_a + beta - 1) / beta, nbs = (bits_b + beta - 1) / beta;
-  const int wa = (m * nb * 32 + 255) / 256, wb = (n * nb * 32 + 255) / 256;
-  exponent_kernel<TA><<<wa, 256, 0, st>>>(A, sA, lda, conjA, m, k, true, ea, nb);
-  exponent_kernel<TB><<<wb, 256, 0, st>>>(B, sB, ldb, false, k, n, false, fb, nb);
-  slice_left_kernel<TA><<<grid_for((size_t)m * k * nb), 256, 0, st>>>(A, sA, lda, conjA, m, k, ea, na, beta, wsA, nb);
-  slice_right_kernel<TB><<<grid_for((size_t)k * n * nb), 256, 0, st>>>(B, sB, ldb, k, n, fb, nbs, beta, wsB, nb);
-  scope.add_launches(4);
-  const float one = 1.0f, zero = 0.0f;
-  const long long bigA = 4LL * m * k, bigB = 2LL * k * n;
-  // products with equal s + t share their scale; up to `group` of them sum
-  // exactly in FP32 before the FP64 accumulation
-  const double qmax = (double)((1 << beta) - 1);
-  const int group = std::max(1, (int)((double)(1 << 24) / (2.0 * k * qmax * qmax)));
-  const int T = (std::max(bits_a, bits_b) + beta - 1) / beta + 1;
-  const dim3 agrid((unsigned)std::min<size_t>(((size_t)m * n + 255) / 256, 152 * 4), (unsigned)nb);
-  bool first = true;
-  for (int d = 0; d <= T; ++d) {
-    int in_group = 0;
-    for (int s = 0; s < na; ++s) {
-      const int t = d - s;
-      if (t < 0 || t >= nbs) continue;
-      const float* beta_g = in_group ? &one : &zero;
-      cublasStatus_t bs = cublasGemmStridedBatchedEx(
-          ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * m, n, 2 * k, &one, wsA + (size_t)s * bigA,
-          CUDA_R_16BF, 2 * m, (long long)na * bigA, wsB + (size_t)t * bigB, CUDA_R_16BF, 2 * k,
-          (long long)nbs * bigB, beta_g, G, CUDA_R_32F, 2 * m, 2LL * m * n, nb, CUBLAS_COMPUTE_32F,
-          CUBLAS_GEMM_DEFAULT);
-      if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "BF16 slice GEMM failed");
-      if (++in_group == group) {
-        ozaki_accumulate_kernel<<<agrid, 256, 0, st>>>(G, ea, fb, m, n, beta * (d + 2), first, C);
-        scope.add_launches(1);
-        first = false;
-        in_group = 0;
-      }
-    }
-    if (in_group) {
-      ozaki_accumulate_kernel<<<agrid, 256, 0, st>>>(G, ea, fb, m, n, beta * (d + 2), first, C);
-      scope.add_launches(1);
-      first = false;
-    }
-  }
-  return cuda_check(cudaGetLastError(), "ozaki kernels");
-}
-
 namespace {
 
 // E = Sh - I (FP32), and the FP32 copy of Hh
@@ -923,36 +715,18 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   }
   cudaFreeAsync(s32, stream);
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
-  __nv_bfloat16 *wsA = nullptr, *wsB = nullptr;
-  float* G = nullptr;
-  int *ea = nullptr, *fb = nullptr;
   double *Y = nullptr, *Hh = nullptr, *Sh = nullptr;
   const int b64 = 48, b32 = 24;        // bits kept of FP64 and FP32 operands
-  const int slmax = max_slices(b64, n);
-  if ((st = cuda_check(cudaMallocAsync((void**)&wsA, 2ULL * slmax * 4 * nn * nk, stream), "malloc slices A"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&wsB, 2ULL * slmax * 2 * nn * nk, stream), "malloc slices B"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&G, 4ULL * 2 * nn * nk, stream), "malloc G"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * n * nk, stream), "malloc ea"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * n * nk, stream), "malloc fb"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&Y, 16ULL * nn * nk, stream), "malloc Y"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&Hh, 16ULL * nn * nk, stream), "malloc Hh"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&Sh, 16ULL * nn * nk, stream), "malloc Sh"))) return st;
   const long long snn = (long long)nn * 2;
   // Y = H X ; Hh = X^H Y
-  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk,
-                                       wsA, wsB, G, ea, fb))) return st;
-  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Hh, nk,
-                                       wsA, wsB, G, ea, fb))) return st;
+  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk))) return st;
+  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Hh, nk))) return st;
   // Y = S X ; Sh = X^H Y
-  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, s, snn, n, false, b64, X, snn, n, b32, Y, nk,
-                                       wsA, wsB, G, ea, fb))) return st;
-  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Sh, nk,
-                                       wsA, wsB, G, ea, fb))) return st;
-  cudaFreeAsync(wsA, stream);
-  cudaFreeAsync(wsB, stream);
-  cudaFreeAsync(G, stream);
-  cudaFreeAsync(ea, stream);
-  cudaFreeAsync(fb, stream);
+  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, s, snn, n, false, b64, X, snn, n, b32, Y, nk))) return st;
+  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Sh, nk))) return st;
   cudaFreeAsync(Y, stream);
   // ---- 3. Loewdin transform: Sh = I + E  ->  (I+F)^H Hh (I+F), F = -E/2 + 3E^2/8
   // so that the pencil is standard; the products with the small F need only
@@ -1032,24 +806,8 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
 // Error-free product check entry (tests): C = A B for one complex FP64 pair.
 int ozaki_selftest(olc_context* ctx, int m, int n, int k, const double* A, const double* B,
                    double* C) {
-  __nv_bfloat16 *wsA = nullptr, *wsB = nullptr;
-  float* G = nullptr;
-  int *ea = nullptr, *fb = nullptr;
-  int st;
-  cudaStream_t stream = ctx->stream;
-  const int sl = max_slices(53, k);
-  if ((st = cuda_check(cudaMallocAsync((void**)&wsA, 2ULL * sl * 4 * m * k, stream), "malloc"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&wsB, 2ULL * sl * 2 * k * n, stream), "malloc"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&G, 4ULL * 2 * m * n, stream), "malloc"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * m, stream), "malloc"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * n, stream), "malloc"))) return st;
-  st = ozaki_zgemm<double, double>(ctx, m, n, k, A, 0, m, false, 53, B, 0, k, 53, C, 1, wsA, wsB, G, ea, fb);
-  cudaFreeAsync(wsA, stream);
-  cudaFreeAsync(wsB, stream);
-  cudaFreeAsync(G, stream);
-  cudaFreeAsync(ea, stream);
-  cudaFreeAsync(fb, stream);
-  int s2 = cuda_check(cudaStreamSynchronize(stream), "ozaki selftest sync");
+  int st = ozaki_zgemm<double, double>(ctx, m, n, k, A, 0, m, false, 53, B, 0, k, 53, C, 1);
+  int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "split product selftest sync");
   return st ? st : s2;
 }
 
