@@ -36,7 +36,7 @@ namespace olc {
 
 namespace {
 
-constexpr int kTrdThreads = 512;
+constexpr int kTrdThreads = 1024;
 constexpr int kWyBlock = 64;         // reflectors per compact-WY block
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -61,11 +61,34 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
 // ---------------------------------------------------------------------------
 // 2. Householder tridiagonalisation, one cluster of G CTAs per k
 // ---------------------------------------------------------------------------
-// A: [nk][n][n] complex FP32, column-major, full Hermitian.  On return
-// column i holds v_i in rows i+1..n-1 (v_i(i+1) = 1), d[k][i] the diagonal of
-// T, e[k][i] its (real) off-diagonal, tau[k][i] the reflector factors.
-// Column r belongs to CTA r % G of the cluster for the whole reduction, so
-// only the cluster's shared memory crosses CTAs.
+// A: [nk][n][n] complex FP32, column-major; only the lower triangle is read
+// or written.  On return column i holds v_i in rows i+1..n-1 (v_i(i+1) = 1),
+// d[k][i] the diagonal of T, e[k][i] its (real) off-diagonal, tau[k][i] the
+// reflector factors.  Column r belongs to CTA r % G of the cluster for the
+// whole reduction, so only the cluster's shared memory crosses CTAs.
+//
+// Step i: (a) the owner of column i applies the pending update of step i-1
+// to it and forms the reflector (v_i, tau_i), broadcast to every CTA;
+// (b) each CTA streams its columns r > i once: element a = A(c, r), c >= r,
+// receives the pending update a -= v_{i-1}(c) conj(w_{i-1}(r)) +
+// w_{i-1}(c) conj(v_{i-1}(r)), is written back, and adds conj(a) v_i(c) to
+// (A v_i)(r) and, for c > r, a v_i(r) to (A v_i)(c) (shared-memory atomics);
+// (c) the partial products are summed over the cluster, p = tau_i A v_i, and
+// w_i = p - tau_i/2 (p^H v_i) v_i becomes the pending update.
+constexpr int kTrdUnroll = 4;
+
+__device__ __forceinline__ void trd_element(float2& a, float2 vp, float2 wp, float2 vc, float2 cw,
+                                            float2 cv, bool pend, float& ax, float& ay) {
+  if (pend) {
+    const float2 t1 = cmul(vp, cw), t2 = cmul(wp, cv);
+    a.x -= t1.x + t2.x;
+    a.y -= t1.y + t2.y;
+  }
+  ax += a.x * vc.x + a.y * vc.y;       // conj(a) v
+  ay += a.x * vc.y - a.y * vc.x;
+}
+
+template <bool VEC>
 __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__ A, int n,
                                                             double* __restrict__ dout,
                                                             double* __restrict__ eout,
@@ -76,17 +99,21 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
   const int k = blockIdx.y;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   float2* Ak = A + (size_t)k * n * n;
-  extern __shared__ float2 trd_sm[];
+  extern __shared__ float4 trd_sm4[];
+  float2* trd_sm = reinterpret_cast<float2*>(trd_sm4);
   __shared__ double red[40];
   __shared__ float2 s_tau, s_scale;
+  for (int e = tid; e < 4 * n; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  cl.sync();
   int cur = 0;
   bool pend = false;
   for (int i = 0; i < n - 1; ++i) {
-    float2* vC = trd_sm + (size_t)(2 * cur) * n;       // v_i
-    float2* wC = trd_sm + (size_t)(2 * cur + 1) * n;   // p_i, then w_i
-    const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;      // pending v_{i-1}
-    const float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;  // pending w_{i-1}
-    // ---- (a) owner of column i: pending update, reflector of column i ------
+    float2* vC = trd_sm + (size_t)(2 * cur) * n;        // v_i
+    float2* wC = trd_sm + (size_t)(2 * cur + 1) * n;    // partial A v_i, then w_i
+    const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;   // pending v_{i-1}
+    float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;     // pending w_{i-1}
+    // ---- (a) owner of column i --------------------------------------------
     if (rank == i % G) {
       float2* col = Ak + (size_t)i * n;
       float2 cw = make_float2(0.f, 0.f), cv = cw;
@@ -133,7 +160,7 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       }
     }
     cl.sync();
-    // ---- (b) one pass over the owned trailing columns ----------------------
+    // ---- (b) one pass over the owned columns' lower parts -------------------
     const float2 tau = s_tau;
     int r0 = i + 1;
     r0 += ((rank - r0) % G + G) % G;
@@ -141,49 +168,110 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       float2* col = Ak + (size_t)r * n;
       float2 cw = make_float2(0.f, 0.f), cv = cw;
       if (pend) { cw = conjf2(wP[r]); cv = conjf2(vP[r]); }
+      const float2 vr = vC[r];
       float ax = 0.f, ay = 0.f;
-      int c = i + 1 + lane;
-      for (; c + 96 < n; c += 128) {
-        float2 a[4];
+      if (VEC) {
+        // rows in pairs (2q, 2q+1); rows above the diagonal are masked
+        float4* col4 = reinterpret_cast<float4*>(col);
+        const float4* vP4 = reinterpret_cast<const float4*>(vP);
+        const float4* wP4 = reinterpret_cast<const float4*>(wP);
+        const float4* vC4 = reinterpret_cast<const float4*>(vC);
+        const int q1 = n >> 1;
+        int q = (r >> 1) + lane;
+        for (; q + 32 * (kTrdUnroll - 1) < q1; q += 32 * kTrdUnroll) {
+          float4 a4[kTrdUnroll];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] = col[c + 32 * u];
+          for (int u = 0; u < kTrdUnroll; ++u) a4[u] = col4[q + 32 * u];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int cc = c + 32 * u;
-          if (pend) {
-            const float2 t1 = cmul(vP[cc], cw), t2 = cmul(wP[cc], cv);
-            a[u].x -= t1.x + t2.x;
-            a[u].y -= t1.y + t2.y;
-            col[cc] = a[u];
+          for (int u = 0; u < kTrdUnroll; ++u) {
+            const int qq = q + 32 * u, c0 = 2 * qq;
+            const float4 vp = vP4[qq], wp = wP4[qq], vc = vC4[qq];
+            float2 a0 = make_float2(a4[u].x, a4[u].y), a1 = make_float2(a4[u].z, a4[u].w);
+            const bool m0 = c0 >= r;
+            float bx = 0.f, by = 0.f;
+            trd_element(a0, make_float2(vp.x, vp.y), make_float2(wp.x, wp.y), make_float2(vc.x, vc.y), cw, cv,
+                        pend, bx, by);
+            trd_element(a1, make_float2(vp.z, vp.w), make_float2(wp.z, wp.w), make_float2(vc.z, vc.w), cw, cv,
+                        pend, ax, ay);
+            if (m0) { ax += bx; ay += by; }
+            if (pend) {
+              if (m0) col4[qq] = make_float4(a0.x, a0.y, a1.x, a1.y);
+              else col[c0 + 1] = a1;
+            }
+            if (c0 > r) {
+              atomicAdd(&wC[c0].x, a0.x * vr.x - a0.y * vr.y);
+              atomicAdd(&wC[c0].y, a0.x * vr.y + a0.y * vr.x);
+            }
+            if (c0 + 1 > r) {
+              atomicAdd(&wC[c0 + 1].x, a1.x * vr.x - a1.y * vr.y);
+              atomicAdd(&wC[c0 + 1].y, a1.x * vr.y + a1.y * vr.x);
+            }
           }
-          const float2 v = vC[cc];
-          ax += a[u].x * v.x + a[u].y * v.y;       // conj(a) v
-          ay += a[u].x * v.y - a[u].y * v.x;
         }
-      }
-      for (; c < n; c += 32) {
-        float2 a = col[c];
-        if (pend) {
-          const float2 t1 = cmul(vP[c], cw), t2 = cmul(wP[c], cv);
-          a.x -= t1.x + t2.x;
-          a.y -= t1.y + t2.y;
-          col[c] = a;
+        for (; q < q1; q += 32) {
+          const int c0 = 2 * q;
+          const float4 a4 = col4[q];
+          const float4 vp = vP4[q], wp = wP4[q], vc = vC4[q];
+          float2 a0 = make_float2(a4.x, a4.y), a1 = make_float2(a4.z, a4.w);
+          const bool m0 = c0 >= r;
+          float bx = 0.f, by = 0.f;
+          trd_element(a0, make_float2(vp.x, vp.y), make_float2(wp.x, wp.y), make_float2(vc.x, vc.y), cw, cv,
+                      pend, bx, by);
+          trd_element(a1, make_float2(vp.z, vp.w), make_float2(wp.z, wp.w), make_float2(vc.z, vc.w), cw, cv,
+                      pend, ax, ay);
+          if (m0) { ax += bx; ay += by; }
+          if (pend) {
+            if (m0) col4[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
+            else col[c0 + 1] = a1;
+          }
+          if (c0 > r) {
+            atomicAdd(&wC[c0].x, a0.x * vr.x - a0.y * vr.y);
+            atomicAdd(&wC[c0].y, a0.x * vr.y + a0.y * vr.x);
+          }
+          if (c0 + 1 > r) {
+            atomicAdd(&wC[c0 + 1].x, a1.x * vr.x - a1.y * vr.y);
+            atomicAdd(&wC[c0 + 1].y, a1.x * vr.y + a1.y * vr.x);
+          }
         }
-        const float2 v = vC[c];
-        ax += a.x * v.x + a.y * v.y;
-        ay += a.x * v.y - a.y * v.x;
+      } else {
+        for (int c = r + lane; c < n; c += 32) {
+          float2 a = col[c];
+          trd_element(a, vP[c], wP[c], vC[c], cw, cv, pend, ax, ay);
+          if (pend) col[c] = a;
+          if (c > r) {
+            atomicAdd(&wC[c].x, a.x * vr.x - a.y * vr.y);
+            atomicAdd(&wC[c].y, a.x * vr.y + a.y * vr.x);
+          }
+        }
       }
       for (int o = 16; o; o >>= 1) {
         ax += __shfl_xor_sync(0xffffffffu, ax, o);
         ay += __shfl_xor_sync(0xffffffffu, ay, o);
       }
       if (lane == 0) {
-        const float2 p = cmul(tau, make_float2(ax, ay));
-        for (int g = 0; g < G; ++g) cl.map_shared_rank(wC, g)[r] = p;
+        atomicAdd(&wC[r].x, ax);
+        atomicAdd(&wC[r].y, ay);
+      }
+    }
+    __syncthreads();
+    cl.sync();
+    // ---- (c) cluster sum of the partial products, p = tau A v ---------------
+    {
+      int c0 = i + 1;
+      c0 += ((rank - c0) % G + G) % G;
+      for (int c = c0 + tid * G; c < n; c += blockDim.x * G) {
+        float2 t = make_float2(0.f, 0.f);
+        for (int g = 0; g < G; ++g) {
+          const float2 u = cl.map_shared_rank(wC, g)[c];
+          t.x += u.x;
+          t.y += u.y;
+        }
+        t = cmul(tau, t);
+        for (int g = 0; g < G; ++g) cl.map_shared_rank(wC, g)[c] = t;
       }
     }
     cl.sync();
-    // ---- (c) w_i = p + alpha v, alpha = -tau/2 (p^H v) ----------------------
+    // w_i = p + alpha v, alpha = -tau/2 (p^H v); clear the next partial buffer
     double sx = 0.0, sy = 0.0;
     for (int c = i + 1 + tid; c < n; c += blockDim.x) {
       const float2 p = wC[c], v = vC[c];
@@ -199,6 +287,7 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       wC[c].x += t.x;
       wC[c].y += t.y;
     }
+    for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
     __syncthreads();
     pend = true;
     cur ^= 1;
@@ -503,8 +592,9 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     int G = 1;
     while (G < 8 && (G * 2) * nk <= 152) G *= 2;
     const size_t smem = 4 * sizeof(float2) * (size_t)n;
-    if ((st = cuda_check(cudaFuncSetAttribute(hetrd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem), "hetrd smem"))) return st;
+    auto kern = (n % 2 == 0) ? hetrd_kernel<true> : hetrd_kernel<false>;
+    if ((st = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "hetrd smem"))) return st;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(G, nk, 1);
     cfg.blockDim = dim3(kTrdThreads, 1, 1);
@@ -517,7 +607,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if ((st = cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel, H, n, d, e, tau), "hetrd launch"))) return st;
+    if ((st = cuda_check(cudaLaunchKernelEx(&cfg, kern, H, n, d, e, tau), "hetrd launch"))) return st;
   }
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
   const size_t T = (size_t)n * nk;
