@@ -36,7 +36,7 @@ namespace olc {
 
 namespace {
 
-constexpr int kTrdThreads = 1024;
+constexpr int kTrdThreads = 512;
 constexpr int kWyBlock = 64;         // reflectors per compact-WY block
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -75,7 +75,7 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
 // (A v_i)(r) and, for c > r, a v_i(r) to (A v_i)(c) (shared-memory atomics);
 // (c) the partial products are summed over the cluster, p = tau_i A v_i, and
 // w_i = p - tau_i/2 (p^H v_i) v_i becomes the pending update.
-constexpr int kTrdUnroll = 4;
+constexpr int kTrdPanel = 8;      // owned columns per warp and pass
 
 __device__ __forceinline__ void trd_element(float2& a, float2 vp, float2 wp, float2 vc, float2 cw,
                                             float2 cv, bool pend, float& ax, float& ay) {
@@ -164,76 +164,96 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
     const float2 tau = s_tau;
     int r0 = i + 1;
     r0 += ((rank - r0) % G + G) % G;
-    for (int r = r0 + warp * G; r < n; r += nwarps * G) {
-      float2* col = Ak + (size_t)r * n;
-      float2 cw = make_float2(0.f, 0.f), cv = cw;
-      if (pend) { cw = conjf2(wP[r]); cv = conjf2(vP[r]); }
-      const float2 vr = vC[r];
-      float ax = 0.f, ay = 0.f;
-      if (VEC) {
-        // rows in pairs (2q, 2q+1); rows above the diagonal are masked
-        float4* col4 = reinterpret_cast<float4*>(col);
-        const float4* vP4 = reinterpret_cast<const float4*>(vP);
-        const float4* wP4 = reinterpret_cast<const float4*>(wP);
-        const float4* vC4 = reinterpret_cast<const float4*>(vC);
-        const int q1 = n >> 1;
-        int q = (r >> 1) + lane;
-        for (; q + 32 * (kTrdUnroll - 1) < q1; q += 32 * kTrdUnroll) {
-          float4 a4[kTrdUnroll];
+    if (VEC) {
+      // panels of kTrdPanel owned columns per warp; lane-owned row pairs
+      // (2q, 2q+1) collect the mirrored products of the whole panel in
+      // registers before one shared-memory atomic
+      const int nown = r0 < n ? (n - r0 + G - 1) / G : 0;
+      const int npanel = (nown + kTrdPanel - 1) / kTrdPanel;
+      const float4* vP4 = reinterpret_cast<const float4*>(vP);
+      const float4* wP4 = reinterpret_cast<const float4*>(wP);
+      const float4* vC4 = reinterpret_cast<const float4*>(vC);
+      const int q1 = n >> 1;
+      for (int pn = warp; pn < npanel; pn += nwarps) {
+        const int j0 = pn * kTrdPanel;
+        int cr[kTrdPanel];
+        float2 vr[kTrdPanel];
+        float ax[kTrdPanel], ay[kTrdPanel];
 #pragma unroll
-          for (int u = 0; u < kTrdUnroll; ++u) a4[u] = col4[q + 32 * u];
-#pragma unroll
-          for (int u = 0; u < kTrdUnroll; ++u) {
-            const int qq = q + 32 * u, c0 = 2 * qq;
-            const float4 vp = vP4[qq], wp = wP4[qq], vc = vC4[qq];
-            float2 a0 = make_float2(a4[u].x, a4[u].y), a1 = make_float2(a4[u].z, a4[u].w);
-            const bool m0 = c0 >= r;
-            float bx = 0.f, by = 0.f;
-            trd_element(a0, make_float2(vp.x, vp.y), make_float2(wp.x, wp.y), make_float2(vc.x, vc.y), cw, cv,
-                        pend, bx, by);
-            trd_element(a1, make_float2(vp.z, vp.w), make_float2(wp.z, wp.w), make_float2(vc.z, vc.w), cw, cv,
-                        pend, ax, ay);
-            if (m0) { ax += bx; ay += by; }
-            if (pend) {
-              if (m0) col4[qq] = make_float4(a0.x, a0.y, a1.x, a1.y);
-              else col[c0 + 1] = a1;
-            }
-            if (c0 > r) {
-              atomicAdd(&wC[c0].x, a0.x * vr.x - a0.y * vr.y);
-              atomicAdd(&wC[c0].y, a0.x * vr.y + a0.y * vr.x);
-            }
-            if (c0 + 1 > r) {
-              atomicAdd(&wC[c0 + 1].x, a1.x * vr.x - a1.y * vr.y);
-              atomicAdd(&wC[c0 + 1].y, a1.x * vr.y + a1.y * vr.x);
-            }
-          }
+        for (int t = 0; t < kTrdPanel; ++t) {
+          const int j = j0 + t;
+          cr[t] = j < nown ? r0 + j * G : n;          // n marks an empty slot
+          vr[t] = vC[min(cr[t], n - 1)];
+          ax[t] = 0.f;
+          ay[t] = 0.f;
         }
-        for (; q < q1; q += 32) {
+        for (int q = (cr[0] >> 1) + lane; q < q1; q += 32) {
           const int c0 = 2 * q;
-          const float4 a4 = col4[q];
+          float4 a4[kTrdPanel];
+#pragma unroll
+          for (int t = 0; t < kTrdPanel; ++t)
+            a4[t] = (cr[t] <= c0 + 1) ? reinterpret_cast<const float4*>(Ak + (size_t)cr[t] * n)[q]
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
           const float4 vp = vP4[q], wp = wP4[q], vc = vC4[q];
-          float2 a0 = make_float2(a4.x, a4.y), a1 = make_float2(a4.z, a4.w);
-          const bool m0 = c0 >= r;
-          float bx = 0.f, by = 0.f;
-          trd_element(a0, make_float2(vp.x, vp.y), make_float2(wp.x, wp.y), make_float2(vc.x, vc.y), cw, cv,
-                      pend, bx, by);
-          trd_element(a1, make_float2(vp.z, vp.w), make_float2(wp.z, wp.w), make_float2(vc.z, vc.w), cw, cv,
-                      pend, ax, ay);
-          if (m0) { ax += bx; ay += by; }
-          if (pend) {
-            if (m0) col4[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
-            else col[c0 + 1] = a1;
+          const float2 vp0 = make_float2(vp.x, vp.y), vp1 = make_float2(vp.z, vp.w);
+          const float2 wp0 = make_float2(wp.x, wp.y), wp1 = make_float2(wp.z, wp.w);
+          const float2 vc0 = make_float2(vc.x, vc.y), vc1 = make_float2(vc.z, vc.w);
+          float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f;
+#pragma unroll
+          for (int t = 0; t < kTrdPanel; ++t) {
+            if (cr[t] > c0 + 1) continue;            // pair above this column's diagonal
+            float2 a0 = make_float2(a4[t].x, a4[t].y), a1 = make_float2(a4[t].z, a4[t].w);
+            const bool m0 = c0 >= cr[t];
+            float bx = 0.f, by = 0.f;
+            // pending-update coefficients of this column (shared-memory broadcast)
+            const float2 cw = pend ? conjf2(wP[cr[t]]) : make_float2(0.f, 0.f);
+            const float2 cv = pend ? conjf2(vP[cr[t]]) : make_float2(0.f, 0.f);
+            trd_element(a0, vp0, wp0, vc0, cw, cv, pend, bx, by);
+            trd_element(a1, vp1, wp1, vc1, cw, cv, pend, ax[t], ay[t]);
+            if (m0) { ax[t] += bx; ay[t] += by; }
+            float2* colt = Ak + (size_t)cr[t] * n;
+            if (pend) {
+              if (m0) reinterpret_cast<float4*>(colt)[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
+              else colt[c0 + 1] = a1;
+            }
+            if (c0 > cr[t]) {
+              s0x += a0.x * vr[t].x - a0.y * vr[t].y;
+              s0y += a0.x * vr[t].y + a0.y * vr[t].x;
+            }
+            if (c0 + 1 > cr[t]) {
+              s1x += a1.x * vr[t].x - a1.y * vr[t].y;
+              s1y += a1.x * vr[t].y + a1.y * vr[t].x;
+            }
           }
-          if (c0 > r) {
-            atomicAdd(&wC[c0].x, a0.x * vr.x - a0.y * vr.y);
-            atomicAdd(&wC[c0].y, a0.x * vr.y + a0.y * vr.x);
+          if (s0x != 0.f || s0y != 0.f) {
+            atomicAdd(&wC[c0].x, s0x);
+            atomicAdd(&wC[c0].y, s0y);
           }
-          if (c0 + 1 > r) {
-            atomicAdd(&wC[c0 + 1].x, a1.x * vr.x - a1.y * vr.y);
-            atomicAdd(&wC[c0 + 1].y, a1.x * vr.y + a1.y * vr.x);
+          if (s1x != 0.f || s1y != 0.f) {
+            atomicAdd(&wC[c0 + 1].x, s1x);
+            atomicAdd(&wC[c0 + 1].y, s1y);
           }
         }
-      } else {
+#pragma unroll
+        for (int t = 0; t < kTrdPanel; ++t) {
+          float x = ax[t], y = ay[t];
+          for (int o = 16; o; o >>= 1) {
+            x += __shfl_xor_sync(0xffffffffu, x, o);
+            y += __shfl_xor_sync(0xffffffffu, y, o);
+          }
+          if (lane == 0 && cr[t] < n) {
+            atomicAdd(&wC[cr[t]].x, x);
+            atomicAdd(&wC[cr[t]].y, y);
+          }
+        }
+      }
+    } else {
+      for (int r = r0 + warp * G; r < n; r += nwarps * G) {
+        float2* col = Ak + (size_t)r * n;
+        float2 cw = make_float2(0.f, 0.f), cv = cw;
+        if (pend) { cw = conjf2(wP[r]); cv = conjf2(vP[r]); }
+        const float2 vr = vC[r];
+        float ax = 0.f, ay = 0.f;
         for (int c = r + lane; c < n; c += 32) {
           float2 a = col[c];
           trd_element(a, vP[c], wP[c], vC[c], cw, cv, pend, ax, ay);
@@ -243,14 +263,14 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
             atomicAdd(&wC[c].y, a.x * vr.y + a.y * vr.x);
           }
         }
-      }
-      for (int o = 16; o; o >>= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-      }
-      if (lane == 0) {
-        atomicAdd(&wC[r].x, ax);
-        atomicAdd(&wC[r].y, ay);
+        for (int o = 16; o; o >>= 1) {
+          ax += __shfl_xor_sync(0xffffffffu, ax, o);
+          ay += __shfl_xor_sync(0xffffffffu, ay, o);
+        }
+        if (lane == 0) {
+          atomicAdd(&wC[r].x, ax);
+          atomicAdd(&wC[r].y, ay);
+        }
       }
     }
     __syncthreads();
