@@ -1,4 +1,5 @@
 // C ABI of libolcao_gb300 (declared in include/olcao_gpu.h).
+#include <cstdlib>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -118,6 +119,20 @@ int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
   }
   cublasSetStream(ctx->blas, ctx->stream);
   cusolverDnSetStream(ctx->solver, ctx->stream);
+  // FP32 products of the mixed solver run as BF16x9 tensor-core emulation
+  // (FP32 accuracy) unless OLC_FP32_GEMM=simt
+  if (cublasCreate(&ctx->blas_f32) != CUBLAS_STATUS_SUCCESS) {
+    olc_destroy(ctx);
+    return fail(OLC_ERR_CUDA, "cublasCreate failed");
+  }
+  cublasSetStream(ctx->blas_f32, ctx->stream);
+  {
+    const char* v = std::getenv("OLC_FP32_GEMM");
+    if (!(v && std::string(v) == "simt")) {
+      cublasSetMathMode(ctx->blas_f32, CUBLAS_FP32_EMULATED_BF16X9_MATH);
+      cublasSetEmulationStrategy(ctx->blas_f32, CUBLAS_EMULATION_STRATEGY_EAGER);
+    }
+  }
   st = build_system(ctx, sys);
   if (!st) st = build_phase_table(ctx);
   if (!st) st = cuda_check(cudaStreamSynchronize(ctx->stream), "olc_create sync");
@@ -155,6 +170,7 @@ int olc_destroy(olc_context_t* ctx) {
   }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->blas) cublasDestroy(ctx->blas);
+  if (ctx->blas_f32) cublasDestroy(ctx->blas_f32);
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
   delete ctx;
   return OLC_OK;
@@ -170,6 +186,7 @@ int olc_set_stream(olc_context_t* ctx, void* stream) {
   if (!ctx) return fail(OLC_ERR_ARG, "olc_set_stream: null context");
   ctx->stream = static_cast<cudaStream_t>(stream);
   cublasSetStream(ctx->blas, ctx->stream);
+  if (ctx->blas_f32) cublasSetStream(ctx->blas_f32, ctx->stream);
   cusolverDnSetStream(ctx->solver, ctx->stream);
   return OLC_OK;
 }

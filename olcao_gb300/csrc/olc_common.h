@@ -110,6 +110,7 @@ struct olc_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   cublasHandle_t blas = nullptr;
+  cublasHandle_t blas_f32 = nullptr;   // FP32 products (BF16x9 emulation)
   cusolverDnHandle_t solver = nullptr;
   // host copies
   olc_dims_t dims{};

@@ -581,7 +581,7 @@ int loewdin(olc_context* ctx, int n, int nk, double* Hh, double* Sh, float* X) {
   auto* Xc = reinterpret_cast<cuComplex*>(X);
   const long long sn = (long long)nn;
   auto gemm = [&](cublasOperation_t ta, const cuComplex* A, const cuComplex* B, cuComplex* C) {
-    return cublasCgemmStridedBatched(ctx->blas, ta, CUBLAS_OP_N, n, n, n, &one, A, n, sn, B, n, sn,
+    return cublasCgemmStridedBatched(ctx->blas_f32, ta, CUBLAS_OP_N, n, n, n, &one, A, n, sn, B, n, sn,
                                      &zero, C, n, sn, nk);
   };
   if (gemm(CUBLAS_OP_N, Ec, Ec, Fc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm E^2 failed");

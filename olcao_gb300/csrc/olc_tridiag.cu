@@ -669,17 +669,17 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
       const int L = n - j0 - 1;
       const long long sV = (long long)nbb * L, sG = (long long)nbb * nbb, sW = (long long)nbb * n;
       build_v_kernel<<<std::min<size_t>((sV * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, j0, nbb, L, nk, V);
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
+      if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
                                     &zero, Gc, nbb, sG, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H V failed");
       tfactor_kernel<<<nk, 64, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
+      if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
                                     Zx + j0 + 1, n, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H Z failed");
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, nbb, n, nbb, &one, Tc, nbb, sG,
+      if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_N, CUBLAS_OP_N, nbb, n, nbb, &one, Tc, nbb, sG,
                                     W1c, nbb, sW, &zero, W2c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm T W failed");
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, L, n, nbb, &mone, Vc, L, sV,
+      if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_N, CUBLAS_OP_N, L, n, nbb, &mone, Vc, L, sV,
                                     W2c, nbb, sW, &one, Zx + j0 + 1, n, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm Z -= V W failed");
       scope.add_launches(2);
