@@ -716,7 +716,10 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   cudaFreeAsync(s32, stream);
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
   double *Y = nullptr, *Hh = nullptr, *Sh = nullptr;
-  const int b64 = 48, b32 = 24;        // bits kept of FP64 and FP32 operands
+  // bits kept of FP64 and FP32 operands (OLC_SPLIT_BITS overrides the FP64 count)
+  int b64 = 48;
+  const int b32 = 24;
+  if (const char* v = std::getenv("OLC_SPLIT_BITS")) b64 = std::max(24, std::min(53, std::atoi(v)));
   if ((st = cuda_check(cudaMallocAsync((void**)&Y, 16ULL * nn * nk, stream), "malloc Y"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&Hh, 16ULL * nn * nk, stream), "malloc Hh"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&Sh, 16ULL * nn * nk, stream), "malloc Sh"))) return st;

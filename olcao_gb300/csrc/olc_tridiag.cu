@@ -16,7 +16,7 @@
 //      eigenvectors by FP64 inverse iteration (LU with partial pivoting of
 //      T - sigma I, as LAPACK dstein), then modified Gram-Schmidt inside every
 //      group of eigenvalues too close for inverse iteration to separate.
-//   4. Back-transform Z = Q Z_T in blocks of 64 reflectors written as
+//   4. Back-transform Z = Q Z_T in blocks of 128 reflectors written as
 //      I - V T V^H (compact WY, LAPACK clarft), three strided-batched GEMMs
 //      per block.
 //   5. X = U^{-1} Z (cuBLAS batched triangular solve).
@@ -37,7 +37,7 @@ namespace olc {
 namespace {
 
 constexpr int kTrdThreads = 512;
-constexpr int kWyBlock = 64;         // reflectors per compact-WY block
+constexpr int kWyBlock = 128;        // reflectors per compact-WY block
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -330,43 +330,71 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
 // ---------------------------------------------------------------------------
 // 3. tridiagonal eigen-solve
 // ---------------------------------------------------------------------------
-// Eigenvalue j (ascending) of T_k by bisection on Sturm counts (FP32): the
+// FP32 copies of T_k for the Sturm counts: df = d, ef = |e| (ef[n-1] = 0).
+__global__ void tri_prep_kernel(const double* __restrict__ d, const double* __restrict__ e, int n,
+                                int nk, float* __restrict__ df, float* __restrict__ ef) {
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)n * nk) return;
+  const int k = (int)(t / n), i = (int)(t % n);
+  df[t] = (float)d[t];
+  ef[t] = i < n - 1 ? fabsf((float)e[(size_t)k * (n - 1) + i]) : 0.f;
+}
+
+// Eigenvalue j (ascending) of T_k by multisection on Sturm counts (FP32): the
 // count of eigenvalues below x is the number of negative pivots of the LDL^T
 // factorisation of T - x I (q_i = d_i - x - e_{i-1}^2 / q_{i-1}, pivots below
-// pivmin replaced by -pivmin as in LAPACK dstebz).
-__global__ void bisect_kernel(const double* __restrict__ d, const double* __restrict__ e, int n,
+// pivmin replaced by -pivmin as in LAPACK dstebz).  Four shifts per pass
+// (four independent recurrences in flight) cut the interval five-fold.
+__global__ void bisect_kernel(const float* __restrict__ df, const float* __restrict__ ef, int n,
                               int nk, double* __restrict__ lam) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * nk) return;
   const int k = t / n, j = t % n;
-  const double* dk = d + (size_t)k * n;
-  const double* ek = e + (size_t)k * (n - 1);
-  float lo = FLT_MAX, hi = -FLT_MAX, emax2 = 0.f;
+  const float* dk = df + (size_t)k * n;
+  const float* ek = ef + (size_t)k * n;
+  float lo = FLT_MAX, hi = -FLT_MAX, emax2 = 0.f, el = 0.f;
   for (int i = 0; i < n; ++i) {
-    const float el = i > 0 ? fabsf((float)ek[i - 1]) : 0.f, er = i < n - 1 ? fabsf((float)ek[i]) : 0.f;
-    const float di = (float)dk[i];
+    const float er = ek[i], di = dk[i];
     lo = fminf(lo, di - el - er);
     hi = fmaxf(hi, di + el + er);
     emax2 = fmaxf(emax2, er * er);
+    el = er;
   }
   const float pivmin = 1e-30f * fmaxf(1.f, emax2);
   const float w = fmaxf(fabsf(lo), fabsf(hi));
   lo -= 4e-6f * w + 2.f * pivmin;
   hi += 4e-6f * w + 2.f * pivmin;
-  for (int it = 0; it < 80; ++it) {
-    const float mid = 0.5f * (lo + hi);
-    if (hi - lo <= 2.f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)) + pivmin || mid == lo || mid == hi) break;
-    int cnt = 0;
-    float q = (float)dk[0] - mid;
-    if (fabsf(q) < pivmin) q = -pivmin;
-    cnt += q < 0.f;
-    for (int i = 1; i < n; ++i) {
-      const float ei = (float)ek[i - 1];
-      q = (float)dk[i] - mid - ei * ei / q;
-      if (fabsf(q) < pivmin) q = -pivmin;
-      cnt += q < 0.f;
+  for (int it = 0; it < 40; ++it) {
+    if (hi - lo <= 2.f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)) + pivmin) break;
+    const float h = 0.2f * (hi - lo);
+    float x[4], q[4];
+    int c[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      x[s] = lo + h * (float)(s + 1);
+      q[s] = dk[0] - x[s];
+      if (fabsf(q[s]) < pivmin) q[s] = -pivmin;
+      c[s] = q[s] < 0.f;
     }
-    if (cnt > j) hi = mid; else lo = mid;
+    for (int i = 1; i < n; ++i) {
+      const float e2 = ek[i - 1] * ek[i - 1], di = dk[i];
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        q[s] = di - x[s] - e2 / q[s];
+        if (fabsf(q[s]) < pivmin) q[s] = -pivmin;
+        c[s] += q[s] < 0.f;
+      }
+    }
+    float nlo = lo, nhi = hi;
+#pragma unroll
+    for (int s = 3; s >= 0; --s)
+      if (c[s] > j) nhi = x[s];
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+      if (c[s] <= j) nlo = x[s];
+    if (nlo == lo && nhi == hi) break;
+    lo = nlo;
+    hi = nhi;
   }
   lam[t] = 0.5 * ((double)lo + (double)hi);
 }
@@ -402,13 +430,13 @@ __global__ void invit_kernel(const double* __restrict__ d, const double* __restr
     const size_t o = (size_t)i * T + t;
     if (fabs(a) >= fabs(sub)) {
       if (fabs(a) < tiny) a = a >= 0.0 ? tiny : -tiny;
-      const double m = sub / a;
-      U0[o] = 1.0 / a; U1[o] = b; U2[o] = 0.0; Lm[o] = m; piv[o] = 0;
+      const double inv = 1.0 / a, m = sub * inv;
+      U0[o] = inv; U1[o] = b; U2[o] = 0.0; Lm[o] = m; piv[o] = 0;
       a = nd - m * b;
       b = ns;
     } else {
-      const double m = a / sub;
-      U0[o] = 1.0 / sub; U1[o] = nd; U2[o] = ns; Lm[o] = m; piv[o] = 1;
+      const double inv = 1.0 / sub, m = a * inv;
+      U0[o] = inv; U1[o] = nd; U2[o] = ns; Lm[o] = m; piv[o] = 1;
       a = b - m * nd;
       b = -m * ns;
     }
@@ -632,12 +660,16 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
   const size_t T = (size_t)n * nk;
   if ((st = cuda_check(cudaMallocAsync((void**)&lam, 8ULL * T, stream), "malloc lam"))) return st;
+  float *df = nullptr, *ef = nullptr;
+  if ((st = cuda_check(cudaMallocAsync((void**)&df, 4ULL * T, stream), "malloc df"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&ef, 4ULL * T, stream), "malloc ef"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&work, 8ULL * 5 * n * T, stream), "malloc invit work"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&piv, (size_t)n * T, stream), "malloc piv"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&Z, 8ULL * nn * nk, stream), "malloc Z"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
-    bisect_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(d, e, n, nk, lam);
+    tri_prep_kernel<<<(int)((T + 255) / 256), 256, 0, stream>>>(d, e, n, nk, df, ef);
+    bisect_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(df, ef, n, nk, lam);
     invit_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(d, e, lam, n, nk, work, piv, Z);
     const size_t gsm = sizeof(int) * 2 * (size_t)(n / 2 + 1);
     if ((st = cuda_check(cudaFuncSetAttribute(group_mgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -646,6 +678,8 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   }
   cudaFreeAsync(work, stream);
   cudaFreeAsync(piv, stream);
+  cudaFreeAsync(df, stream);
+  cudaFreeAsync(ef, stream);
   // ---- 4. back-transform X = Q Z_T ------------------------------------------
   {
     const int nblk = (n - 1 + kWyBlock - 1) / kWyBlock;
@@ -672,7 +706,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
                                     &zero, Gc, nbb, sG, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H V failed");
-      tfactor_kernel<<<nk, 64, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
+      tfactor_kernel<<<nk, kWyBlock, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
                                     Zx + j0 + 1, n, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H Z failed");
