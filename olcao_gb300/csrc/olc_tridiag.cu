@@ -26,6 +26,7 @@
 #include <cfloat>
 #include <cooperative_groups.h>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "olc_common.h"
@@ -58,6 +59,28 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
   return red[32];
 }
 
+// Two sums over the CTA in FP64 (red: >= 66 doubles).
+__device__ __forceinline__ void block_sum2_d(double& a, double& b, double* red) {
+  for (int o = 16; o; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = a;
+    red[32 + (threadIdx.x >> 5)] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { s += red[q]; t += red[32 + q]; }
+    red[64] = s;
+    red[65] = t;
+  }
+  __syncthreads();
+  a = red[64];
+  b = red[65];
+}
+
 // ---------------------------------------------------------------------------
 // 2. Householder tridiagonalisation, one cluster of G CTAs per k
 // ---------------------------------------------------------------------------
@@ -67,14 +90,16 @@ __device__ __forceinline__ double block_sum_d(double v, double* red) {
 // reflector factors.  Column r belongs to CTA r % G of the cluster for the
 // whole reduction, so only the cluster's shared memory crosses CTAs.
 //
-// Step i: (a) the owner of column i applies the pending update of step i-1
-// to it and forms the reflector (v_i, tau_i), broadcast to every CTA;
+// Step i: (a) every CTA reads column i from L2, applies the pending update
+// of step i-1 and forms the reflector (v_i, tau_i) itself (no broadcast);
 // (b) each CTA streams its columns r > i once: element a = A(c, r), c >= r,
 // receives the pending update a -= v_{i-1}(c) conj(w_{i-1}(r)) +
 // w_{i-1}(c) conj(v_{i-1}(r)), is written back, and adds conj(a) v_i(c) to
 // (A v_i)(r) and, for c > r, a v_i(r) to (A v_i)(c) (shared-memory atomics);
-// (c) the partial products are summed over the cluster, p = tau_i A v_i, and
-// w_i = p - tau_i/2 (p^H v_i) v_i becomes the pending update.
+// (c) the partial products are summed over the cluster, p = tau_i A v_i,
+// together with the shares of p^H v_i, and w_i = p - tau_i/2 (p^H v_i) v_i
+// becomes the pending update; the owner of column i stores v_i there.  Two
+// cluster barriers per step.
 constexpr int kTrdPanel = 8;      // owned columns per warp and pass
 
 __device__ __forceinline__ void trd_element(float2& a, float2 vp, float2 wp, float2 vc, float2 cw,
@@ -86,6 +111,112 @@ __device__ __forceinline__ void trd_element(float2& a, float2 vp, float2 wp, flo
   }
   ax += a.x * vc.x + a.y * vc.y;       // conj(a) v
   ay += a.x * vc.y - a.y * vc.x;
+}
+
+// One row pair (2q, 2q+1) of a panel: pending update, write-back, column
+// products and the pair's mirrored products.  MASK: the pair may lie on or
+// above a panel column's diagonal.
+template <bool PEND, bool MASK>
+__device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int q,
+                                         const int (&cr)[kTrdPanel], const float2* __restrict__ vP,
+                                         const float2* __restrict__ wP, const float2 (&vr)[kTrdPanel],
+                                         float (&ax)[kTrdPanel], float (&ay)[kTrdPanel],
+                                         const float4* __restrict__ vP4, const float4* __restrict__ wP4,
+                                         const float4* __restrict__ vC4, float2* wC) {
+  const int c0 = 2 * q;
+  float4 a4[kTrdPanel];
+#pragma unroll
+  for (int t = 0; t < kTrdPanel; ++t)
+    a4[t] = (cr[t] < n && (!MASK || cr[t] <= c0 + 1))
+                ? reinterpret_cast<const float4*>(Ak + (size_t)cr[t] * n)[q]
+                : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 vc = vC4[q];
+  float4 vp = make_float4(0.f, 0.f, 0.f, 0.f), wp = vp;
+  if (PEND) { vp = vP4[q]; wp = wP4[q]; }
+  float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f;
+#pragma unroll
+  for (int t = 0; t < kTrdPanel; ++t) {
+    if (cr[t] >= n || (MASK && cr[t] > c0 + 1)) continue;
+    float2 a0 = make_float2(a4[t].x, a4[t].y), a1 = make_float2(a4[t].z, a4[t].w);
+    if (PEND) {
+      // conj(w(r)) and conj(v(r)) of this column (shared-memory broadcast)
+      const float2 cw = conjf2(wP[cr[t]]), cv = conjf2(vP[cr[t]]);
+      a0.x -= (vp.x * cw.x - vp.y * cw.y) + (wp.x * cv.x - wp.y * cv.y);
+      a0.y -= (vp.x * cw.y + vp.y * cw.x) + (wp.x * cv.y + wp.y * cv.x);
+      a1.x -= (vp.z * cw.x - vp.w * cw.y) + (wp.z * cv.x - wp.w * cv.y);
+      a1.y -= (vp.z * cw.y + vp.w * cw.x) + (wp.z * cv.y + wp.w * cv.x);
+    }
+    const bool m0 = !MASK || c0 >= cr[t];
+    if (m0) {
+      ax[t] += a0.x * vc.x + a0.y * vc.y;         // conj(a) v
+      ay[t] += a0.x * vc.y - a0.y * vc.x;
+    }
+    ax[t] += a1.x * vc.z + a1.y * vc.w;
+    ay[t] += a1.x * vc.w - a1.y * vc.z;
+    float2* colt = Ak + (size_t)cr[t] * n;
+    if (PEND) {
+      if (m0) reinterpret_cast<float4*>(colt)[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
+      else colt[c0 + 1] = a1;
+    }
+    if (!MASK || c0 > cr[t]) {
+      s0x += a0.x * vr[t].x - a0.y * vr[t].y;
+      s0y += a0.x * vr[t].y + a0.y * vr[t].x;
+    }
+    if (!MASK || c0 + 1 > cr[t]) {
+      s1x += a1.x * vr[t].x - a1.y * vr[t].y;
+      s1y += a1.x * vr[t].y + a1.y * vr[t].x;
+    }
+  }
+  if (!MASK || s0x != 0.f || s0y != 0.f) {
+    atomicAdd(&wC[c0].x, s0x);
+    atomicAdd(&wC[c0].y, s0y);
+  }
+  if (!MASK || s1x != 0.f || s1y != 0.f) {
+    atomicAdd(&wC[c0 + 1].x, s1x);
+    atomicAdd(&wC[c0 + 1].y, s1y);
+  }
+}
+
+// One panel of kTrdPanel owned columns (slots past the last column are
+// empty): the pairs touching the diagonals first, then the bulk unmasked.
+template <bool PEND>
+__device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int r0, int G, int pn, int nown,
+                                          int lane, const float2* vP, const float2* wP, const float2* vC,
+                                          float2* wC) {
+  int cr[kTrdPanel];
+  float2 vr[kTrdPanel];
+  float ax[kTrdPanel], ay[kTrdPanel];
+  int c_last = 0;
+#pragma unroll
+  for (int t = 0; t < kTrdPanel; ++t) {
+    const int j = pn * kTrdPanel + t;
+    cr[t] = j < nown ? r0 + j * G : n;          // n marks an empty slot
+    const int rr = min(cr[t], n - 1);
+    if (cr[t] < n) c_last = cr[t];
+    vr[t] = vC[rr];
+    ax[t] = 0.f;
+    ay[t] = 0.f;
+  }
+  const float4* vP4 = reinterpret_cast<const float4*>(vP);
+  const float4* wP4 = reinterpret_cast<const float4*>(wP);
+  const float4* vC4 = reinterpret_cast<const float4*>(vC);
+  const int q1 = n >> 1;
+  const int qd = min(q1, (c_last >> 1) + 1);    // pairs from qd on lie below every diagonal
+  int q = (cr[0] >> 1) + lane;
+  for (; q < qd; q += 32) trd_pair<PEND, true>(Ak, n, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+  for (; q < q1; q += 32) trd_pair<PEND, false>(Ak, n, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+#pragma unroll
+  for (int t = 0; t < kTrdPanel; ++t) {
+    float x = ax[t], y = ay[t];
+    for (int o = 16; o; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    if (lane == 0 && cr[t] < n) {
+      atomicAdd(&wC[cr[t]].x, x);
+      atomicAdd(&wC[cr[t]].y, y);
+    }
+  }
 }
 
 template <bool VEC>
@@ -101,8 +232,10 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
   float2* Ak = A + (size_t)k * n * n;
   extern __shared__ float4 trd_sm4[];
   float2* trd_sm = reinterpret_cast<float2*>(trd_sm4);
-  __shared__ double red[40];
+  __shared__ double red[72];
   __shared__ float2 s_tau, s_scale;
+  __shared__ float s_diag, s_beta;
+  __shared__ double2 s_dot[16];
   for (int e = tid; e < 4 * n; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
   __syncthreads();
   cl.sync();
@@ -113,9 +246,11 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
     float2* wC = trd_sm + (size_t)(2 * cur + 1) * n;    // partial A v_i, then w_i
     const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;   // pending v_{i-1}
     float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;     // pending w_{i-1}
-    // ---- (a) owner of column i --------------------------------------------
-    if (rank == i % G) {
-      float2* col = Ak + (size_t)i * n;
+    // ---- (a) every CTA: pending update of column i, reflector of column i ----
+    // (column i is read from L2 by all CTAs; its owner writes v_i back only
+    // after the next cluster barrier)
+    {
+      const float2* col = Ak + (size_t)i * n;
       float2 cw = make_float2(0.f, 0.f), cv = cw;
       if (pend) { cw = conjf2(wP[i]); cv = conjf2(vP[i]); }
       double part = 0.0;
@@ -126,7 +261,7 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
           a.x -= t1.x + t2.x;
           a.y -= t1.y + t2.y;
         }
-        if (r == i) dout[(size_t)k * n + i] = a.x;
+        if (r == i) s_diag = a.x;
         else vC[r] = a;
         if (r >= i + 2) part += (double)a.x * a.x + (double)a.y * a.y;
       }
@@ -134,32 +269,24 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       if (tid == 0) {
         const float2 al = vC[i + 1];
         float2 tau = make_float2(0.f, 0.f), scale = make_float2(0.f, 0.f);
-        double beta = al.x;
+        float beta = al.x;
         if (!(xn2 == 0.0 && al.y == 0.f)) {
-          const double an = sqrt((double)al.x * al.x + (double)al.y * al.y + xn2);
+          const float an = sqrtf(al.x * al.x + al.y * al.y + (float)xn2);
           beta = (al.x >= 0.f) ? -an : an;
-          tau = make_float2((float)((beta - al.x) / beta), (float)(-al.y / beta));
-          const double dr = al.x - beta, di = al.y, den = dr * dr + di * di;
-          scale = make_float2((float)(dr / den), (float)(-di / den));
+          tau = make_float2((beta - al.x) / beta, -al.y / beta);
+          const float dr = al.x - beta, di = al.y, den = dr * dr + di * di;
+          scale = make_float2(dr / den, -di / den);
         }
-        eout[(size_t)k * (n - 1) + i] = beta;
-        tout[(size_t)k * (n - 1) + i] = tau;
         s_tau = tau;
         s_scale = scale;
-        for (int g = 0; g < G; ++g)
-          if (g != rank) *cl.map_shared_rank(&s_tau, g) = tau;
+        s_beta = beta;
       }
       __syncthreads();
       const float2 scale = s_scale;
-      for (int r = i + 1 + tid; r < n; r += blockDim.x) {
-        const float2 v = (r == i + 1) ? make_float2(1.f, 0.f) : cmul(vC[r], scale);
-        vC[r] = v;
-        col[r] = v;
-        for (int g = 0; g < G; ++g)
-          if (g != rank) cl.map_shared_rank(vC, g)[r] = v;
-      }
+      for (int r = i + 1 + tid; r < n; r += blockDim.x)
+        vC[r] = (r == i + 1) ? make_float2(1.f, 0.f) : cmul(vC[r], scale);
+      __syncthreads();
     }
-    cl.sync();
     // ---- (b) one pass over the owned columns' lower parts -------------------
     const float2 tau = s_tau;
     int r0 = i + 1;
@@ -170,82 +297,9 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       // registers before one shared-memory atomic
       const int nown = r0 < n ? (n - r0 + G - 1) / G : 0;
       const int npanel = (nown + kTrdPanel - 1) / kTrdPanel;
-      const float4* vP4 = reinterpret_cast<const float4*>(vP);
-      const float4* wP4 = reinterpret_cast<const float4*>(wP);
-      const float4* vC4 = reinterpret_cast<const float4*>(vC);
-      const int q1 = n >> 1;
       for (int pn = warp; pn < npanel; pn += nwarps) {
-        const int j0 = pn * kTrdPanel;
-        int cr[kTrdPanel];
-        float2 vr[kTrdPanel];
-        float ax[kTrdPanel], ay[kTrdPanel];
-#pragma unroll
-        for (int t = 0; t < kTrdPanel; ++t) {
-          const int j = j0 + t;
-          cr[t] = j < nown ? r0 + j * G : n;          // n marks an empty slot
-          vr[t] = vC[min(cr[t], n - 1)];
-          ax[t] = 0.f;
-          ay[t] = 0.f;
-        }
-        for (int q = (cr[0] >> 1) + lane; q < q1; q += 32) {
-          const int c0 = 2 * q;
-          float4 a4[kTrdPanel];
-#pragma unroll
-          for (int t = 0; t < kTrdPanel; ++t)
-            a4[t] = (cr[t] <= c0 + 1) ? reinterpret_cast<const float4*>(Ak + (size_t)cr[t] * n)[q]
-                                      : make_float4(0.f, 0.f, 0.f, 0.f);
-          const float4 vp = vP4[q], wp = wP4[q], vc = vC4[q];
-          const float2 vp0 = make_float2(vp.x, vp.y), vp1 = make_float2(vp.z, vp.w);
-          const float2 wp0 = make_float2(wp.x, wp.y), wp1 = make_float2(wp.z, wp.w);
-          const float2 vc0 = make_float2(vc.x, vc.y), vc1 = make_float2(vc.z, vc.w);
-          float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f;
-#pragma unroll
-          for (int t = 0; t < kTrdPanel; ++t) {
-            if (cr[t] > c0 + 1) continue;            // pair above this column's diagonal
-            float2 a0 = make_float2(a4[t].x, a4[t].y), a1 = make_float2(a4[t].z, a4[t].w);
-            const bool m0 = c0 >= cr[t];
-            float bx = 0.f, by = 0.f;
-            // pending-update coefficients of this column (shared-memory broadcast)
-            const float2 cw = pend ? conjf2(wP[cr[t]]) : make_float2(0.f, 0.f);
-            const float2 cv = pend ? conjf2(vP[cr[t]]) : make_float2(0.f, 0.f);
-            trd_element(a0, vp0, wp0, vc0, cw, cv, pend, bx, by);
-            trd_element(a1, vp1, wp1, vc1, cw, cv, pend, ax[t], ay[t]);
-            if (m0) { ax[t] += bx; ay[t] += by; }
-            float2* colt = Ak + (size_t)cr[t] * n;
-            if (pend) {
-              if (m0) reinterpret_cast<float4*>(colt)[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
-              else colt[c0 + 1] = a1;
-            }
-            if (c0 > cr[t]) {
-              s0x += a0.x * vr[t].x - a0.y * vr[t].y;
-              s0y += a0.x * vr[t].y + a0.y * vr[t].x;
-            }
-            if (c0 + 1 > cr[t]) {
-              s1x += a1.x * vr[t].x - a1.y * vr[t].y;
-              s1y += a1.x * vr[t].y + a1.y * vr[t].x;
-            }
-          }
-          if (s0x != 0.f || s0y != 0.f) {
-            atomicAdd(&wC[c0].x, s0x);
-            atomicAdd(&wC[c0].y, s0y);
-          }
-          if (s1x != 0.f || s1y != 0.f) {
-            atomicAdd(&wC[c0 + 1].x, s1x);
-            atomicAdd(&wC[c0 + 1].y, s1y);
-          }
-        }
-#pragma unroll
-        for (int t = 0; t < kTrdPanel; ++t) {
-          float x = ax[t], y = ay[t];
-          for (int o = 16; o; o >>= 1) {
-            x += __shfl_xor_sync(0xffffffffu, x, o);
-            y += __shfl_xor_sync(0xffffffffu, y, o);
-          }
-          if (lane == 0 && cr[t] < n) {
-            atomicAdd(&wC[cr[t]].x, x);
-            atomicAdd(&wC[cr[t]].y, y);
-          }
-        }
+        if (pend) trd_panel<true>(Ak, n, r0, G, pn, nown, lane, vP, wP, vC, wC);
+        else trd_panel<false>(Ak, n, r0, G, pn, nown, lane, vP, wP, vC, wC);
       }
     } else {
       for (int r = r0 + warp * G; r < n; r += nwarps * G) {
@@ -275,10 +329,12 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
     }
     __syncthreads();
     cl.sync();
-    // ---- (c) cluster sum of the partial products, p = tau A v ---------------
+    // ---- (c) cluster sum of the partial products, p = tau A v, with the
+    // partial p^H v of this CTA's share; w_i = p + alpha v, alpha = -tau/2 p^H v
     {
       int c0 = i + 1;
       c0 += ((rank - c0) % G + G) % G;
+      double sx = 0.0, sy = 0.0;
       for (int c = c0 + tid * G; c < n; c += blockDim.x * G) {
         float2 t = make_float2(0.f, 0.f);
         for (int g = 0; g < G; ++g) {
@@ -287,27 +343,38 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
           t.y += u.y;
         }
         t = cmul(tau, t);
+        const float2 v = vC[c];
+        sx += (double)t.x * v.x + (double)t.y * v.y;
+        sy += (double)t.x * v.y - (double)t.y * v.x;
         for (int g = 0; g < G; ++g) cl.map_shared_rank(wC, g)[c] = t;
       }
+      block_sum2_d(sx, sy, red);
+      if (tid == 0)
+        for (int g = 0; g < G; ++g) cl.map_shared_rank(s_dot, g)[rank] = make_double2(sx, sy);
     }
     cl.sync();
-    // w_i = p + alpha v, alpha = -tau/2 (p^H v); clear the next partial buffer
-    double sx = 0.0, sy = 0.0;
-    for (int c = i + 1 + tid; c < n; c += blockDim.x) {
-      const float2 p = wC[c], v = vC[c];
-      sx += (double)p.x * v.x + (double)p.y * v.y;
-      sy += (double)p.x * v.y - (double)p.y * v.x;
+    {
+      double sx = 0.0, sy = 0.0;
+      for (int g = 0; g < G; ++g) { sx += s_dot[g].x; sy += s_dot[g].y; }
+      const float2 al2 = make_float2((float)(-0.5 * (tau.x * sx - tau.y * sy)),
+                                     (float)(-0.5 * (tau.x * sy + tau.y * sx)));
+      for (int c = i + 1 + tid; c < n; c += blockDim.x) {
+        const float2 t = cmul(al2, vC[c]);
+        wC[c].x += t.x;
+        wC[c].y += t.y;
+      }
+      for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
+      // the owner stores the reflector and T's entries
+      if (rank == i % G) {
+        float2* col = Ak + (size_t)i * n;
+        for (int r = i + 1 + tid; r < n; r += blockDim.x) col[r] = vC[r];
+        if (tid == 0) {
+          dout[(size_t)k * n + i] = s_diag;
+          eout[(size_t)k * (n - 1) + i] = s_beta;
+          tout[(size_t)k * (n - 1) + i] = tau;
+        }
+      }
     }
-    sx = block_sum_d(sx, red);
-    sy = block_sum_d(sy, red);
-    const float2 al2 = make_float2((float)(-0.5 * (tau.x * sx - tau.y * sy)),
-                                   (float)(-0.5 * (tau.x * sy + tau.y * sx)));
-    for (int c = i + 1 + tid; c < n; c += blockDim.x) {
-      const float2 t = cmul(al2, vC[c]);
-      wC[c].x += t.x;
-      wC[c].y += t.y;
-    }
-    for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
     __syncthreads();
     pend = true;
     cur ^= 1;
@@ -637,8 +704,13 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   if ((st = cuda_check(cudaMallocAsync((void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 1);
+    // CTAs per k: enough clusters to fill the SMs (OLC_TRD_CLUSTER overrides)
     int G = 1;
     while (G < 8 && (G * 2) * nk <= 152) G *= 2;
+    if (const char* v = std::getenv("OLC_TRD_CLUSTER")) {
+      const int g = std::atoi(v);
+      if (g == 1 || g == 2 || g == 4 || g == 8) G = g;
+    }
     const size_t smem = 4 * sizeof(float2) * (size_t)n;
     auto kern = (n % 2 == 0) ? hetrd_kernel<true> : hetrd_kernel<false>;
     if ((st = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
