@@ -601,8 +601,10 @@ __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict
 // ---------------------------------------------------------------------------
 // 4. compact-WY back-transform
 // ---------------------------------------------------------------------------
-// V block: reflectors j0..j0+nb-1 on rows j0+1..n-1 (L rows), zero above each
-// reflector's leading 1.  V: [nk][nb][L] complex, column-major.
+// V block: reflectors j0..j0+nb-1 on rows j0..n-1 (L rows; row j0 and the
+// rows above each reflector's leading 1 are zero, so that with j0 and n even
+// every GEMM operand starts on a 16-byte boundary).  V: [nk][nb][L] complex,
+// column-major.
 __global__ void build_v_kernel(const float2* __restrict__ A, int n, int j0, int nb, int L,
                                int nk, float2* __restrict__ V) {
   const size_t total = (size_t)nk * nb * L;
@@ -611,7 +613,7 @@ __global__ void build_v_kernel(const float2* __restrict__ A, int n, int j0, int 
     const int rr = (int)(e % L);
     const int tcol = (int)((e / L) % nb);
     const int k = (int)(e / ((size_t)L * nb));
-    const int r = j0 + 1 + rr, j = j0 + tcol;
+    const int r = j0 + rr, j = j0 + tcol;
     V[e] = (r >= j + 1) ? A[(size_t)k * n * n + (size_t)j * n + r] : make_float2(0.f, 0.f);
   }
 }
@@ -772,7 +774,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     for (int b = nblk - 1; b >= 0; --b) {
       const int j0 = b * kWyBlock;
       const int nbb = std::min(kWyBlock, n - 1 - j0);
-      const int L = n - j0 - 1;
+      const int L = n - j0;
       const long long sV = (long long)nbb * L, sG = (long long)nbb * nbb, sW = (long long)nbb * n;
       build_v_kernel<<<std::min<size_t>((sV * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, j0, nbb, L, nk, V);
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
@@ -780,13 +782,13 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
         return fail(OLC_ERR_CUDA, "cgemm V^H V failed");
       tfactor_kernel<<<nk, kWyBlock, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
-                                    Zx + j0 + 1, n, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
+                                    Zx + j0, n, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H Z failed");
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_N, CUBLAS_OP_N, nbb, n, nbb, &one, Tc, nbb, sG,
                                     W1c, nbb, sW, &zero, W2c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm T W failed");
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_N, CUBLAS_OP_N, L, n, nbb, &mone, Vc, L, sV,
-                                    W2c, nbb, sW, &one, Zx + j0 + 1, n, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
+                                    W2c, nbb, sW, &one, Zx + j0, n, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm Z -= V W failed");
       scope.add_launches(2);
     }
