@@ -118,9 +118,8 @@ def measured_peaks():
 
 def shard(nk, world, rank):
     """Contiguous k-range of a rank (the k-point decomposition of the path)."""
-    base, extra = divmod(nk, world)
-    lo = rank * base + min(rank, extra)
-    return lo, lo + base + (1 if rank < extra else 0)
+    from olcao_gb300.kshard import shard_range
+    return shard_range(nk, world, rank)
 
 
 # ---------------------------------------------------------------------------

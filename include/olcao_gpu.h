@@ -261,6 +261,28 @@ int olc_solve_zhegv_noalloc(int n, int nk, const double* packed_h, const double*
                             int num_states, double* eigenvalues, double* vectors,
                             int32_t* info, void* stream);
 
+/* Layout-identical raw writers of the reference's HDF5 datasets (no libhdf5
+ * is linked).  Every dataset becomes <root>/<group>/<name>.bin with its
+ * elements in the dataset's Fortran order as little-endian binary64, and
+ * <root>/manifest.json lists path, dims (Fortran order) and type.
+ *
+ * olc_write_setup_integrals replaces the integral writes of setup-temp.hdf5
+ * (hdf5SetupIntg.F90:86-222; integrals.F90:2693, 2826-2840): for every k,
+ * /atomIntgGroup/atomOverlap/%07d, atomKEOverlap/%07d, atomNucOverlap/%07d
+ * and atomPotOverlap/%07d/%07d (k, term), each (2, vale_dim(vale_dim+1)/2)
+ * upper-packed orthogonalised values.  Needs olc_scf_prepare(...,
+ * OLC_FORM_STORED).
+ *
+ * olc_write_eigen replaces the eigen writes of main-temp.hdf5
+ * (secularEqn.F90:232-270, hdf5MainEval.f90:60-81, hdf5MainEvec.F90:81-119):
+ * /eigenValues/%07d%07d (k, spin) of (num_states) and, when vectors != NULL,
+ * /eigenVectors/real%07d%07d and imag%07d%07d of (vale_dim, num_states).
+ * eigenvalues[num_states, nk] and vectors[vale_dim, num_states, nk] complex
+ * are HOST arrays, as olc_scf_iteration returns them. */
+int olc_write_setup_integrals(olc_context_t* ctx, const char* root);
+int olc_write_eigen(const char* root, int num_kpoints, int spin, int num_states, int vale_dim,
+                    const double* eigenvalues, const double* vectors);
+
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the
  * device.  kind: 1 overlap2CIntg, 2 kinetic2CIntg, 3 nuclear3CIntg,

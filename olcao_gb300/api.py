@@ -45,7 +45,7 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
            "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
-           "olc_split_zgemm")
+           "olc_split_zgemm", "olc_write_setup_integrals", "olc_write_eigen")
 STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve", "refine")
 
 _LIB: Optional[C.CDLL] = None
@@ -93,6 +93,8 @@ def lib() -> C.CDLL:
         L.olc_scf_matrices.argtypes = [vp, dp, i32, dp, dp, i32]
         L.olc_solve_zhegv_noalloc.argtypes = [i32, i32, dp, dp, i32, dp, dp, dp, vp]
         L.olc_split_zgemm.argtypes = [vp, i32, i32, i32, dp, dp, dp]
+        L.olc_write_setup_integrals.argtypes = [vp, C.c_char_p]
+        L.olc_write_eigen.argtypes = [C.c_char_p, i32, i32, i32, i32, dp, dp]
         L.olc_launch_count.restype = C.c_int64
         L.olc_launch_count.argtypes = []
         _LIB = L
@@ -133,6 +135,37 @@ def primitive_batch(kind: int, params: np.ndarray, lmalpha: np.ndarray) -> np.nd
     out = np.zeros((n, 256))
     _check(lib().olc_primitive_batch(kind, n, p.ctypes.data, lm.ctypes.data, out.ctypes.data))
     return out.reshape(n, 16, 16).transpose(0, 2, 1)
+
+
+def write_eigen(root: str, eigenvalues: np.ndarray, vectors: Optional[np.ndarray] = None,
+                spin: int = 1) -> None:
+    """Write eigenvalues [nk, num_states] and (optionally) eigenvectors
+    [nk, num_states, vale_dim] complex in the reference's main-temp.hdf5
+    dataset layout (raw files + manifest.json under root)."""
+    ev = np.ascontiguousarray(eigenvalues, np.float64)
+    nk, ns = ev.shape
+    vp = None
+    nv = ns
+    if vectors is not None:
+        vc = np.ascontiguousarray(vectors, np.complex128)
+        assert vc.shape[:2] == (nk, ns)
+        nv = vc.shape[2]
+        vp = vc.ctypes.data
+    _check(lib().olc_write_eigen(root.encode(), nk, spin, ns, nv, ev.ctypes.data, vp))
+
+
+def read_dataset(root: str, path: str) -> np.ndarray:
+    """One dataset written by the raw writers, as an array of its HDF5 dims
+    (Fortran order), found through root/manifest.json."""
+    import json
+    import os
+    with open(os.path.join(root, "manifest.json")) as f:
+        man = json.load(f)
+    for d in man["datasets"]:
+        if d["path"] == path:
+            data = np.fromfile(os.path.join(root, d["file"]), dtype="<f8")
+            return data.reshape(d["dims"], order="F")
+    raise KeyError(path)
 
 
 class Context:
@@ -250,6 +283,12 @@ class Context:
 
     def scf_prepare(self, precision: int = PREC_FP64, form: int = FORM_FUSED):
         _check(lib().olc_scf_prepare(self.h, precision, form))
+
+    def write_setup_integrals(self, root: str):
+        """Packed orthogonalised S, KE, NP and V_j of every k in the
+        reference's setup-temp.hdf5 dataset layout (after
+        scf_prepare(..., FORM_STORED))."""
+        _check(lib().olc_write_setup_integrals(self.h, root.encode()))
 
     def split_zgemm(self, A, B):
         """FP64-accurate complex product on the tensor cores (device tensors,

@@ -298,4 +298,17 @@ int olc_primitive_batch(int kind, int n, const double* in, const int32_t* lmalph
   return primitive_batch_device(kind, n, in, lmalpha, out);
 }
 
+int olc_write_setup_integrals(olc_context_t* ctx, const char* root) {
+  if (!ctx || !root) return fail(OLC_ERR_ARG, "olc_write_setup_integrals: null argument");
+  return write_setup_integrals(ctx, root);
+}
+
+int olc_write_eigen(const char* root, int num_kpoints, int spin, int num_states, int vale_dim,
+                    const double* eigenvalues, const double* vectors) {
+  if (!root || !eigenvalues || num_kpoints < 1 || spin < 1 || num_states < 1 || vale_dim < 1 ||
+      num_states > vale_dim)
+    return fail(OLC_ERR_ARG, "olc_write_eigen: bad argument");
+  return write_eigen(root, num_kpoints, spin, num_states, vale_dim, eigenvalues, vectors);
+}
+
 }  // extern "C"

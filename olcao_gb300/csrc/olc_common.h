@@ -254,6 +254,11 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
                 int nb);
 void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
 
+// raw layout-identical dataset writer (olc_layout.cu)
+int write_setup_integrals(olc_context* ctx, const char* root);
+int write_eigen(const char* root, int nk, int spin, int num_states, int vale_dim, const double* eig,
+                const double* vectors);
+
 // batched FP32 eigen-solve (olc_tridiag.cu)
 int hetrd_max_n();
 int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X);

@@ -27,3 +27,12 @@ def gpu_lib():
 def golden():
     import numpy as np
     return np.load(os.path.join(ROOT, "tests", "golden", "primitives.npz"))
+
+
+@pytest.fixture(scope="session")
+def gpu_free_lib():
+    """Builds (if stale) and loads the library for its host-only entry points
+    (argument checks, dataset writers); needs no GPU."""
+    from olcao_gb300 import build, api
+    build.build()
+    return api.lib()
