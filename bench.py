@@ -42,6 +42,10 @@ WORKLOADS = {
     "si64": "Si64 2x2x2 diamond supercell, 832 basis fns (320 core), 64 k (4x4x4 MP), "
             "18 Gaussians 0.12-1e6, 16-term potential",
     "diamond": "diamond C 2-atom FCC, 10 basis fns (2 core), 216 k (6x6x6 MP)",
+    "si8": "Si8 conventional cell, valence only, 104 basis fns, 512 k (8x8x8 MP)",
+    "graphite": "AB graphite 4 atoms, valence only, 32 basis fns, 8192 k (32x32x8 MP)",
+    "quartz": "alpha-quartz SiO2 3x3x3 (243 atoms), 3159 basis fns (567 core), 9 k (Gamma + 2x2x2)",
+    "si512": "Si512 4x4x4 diamond supercell, 6656 basis fns (2560 core), 9 k (Gamma + shifted 2x2x2)",
 }
 
 

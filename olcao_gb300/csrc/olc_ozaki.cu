@@ -97,12 +97,13 @@ __global__ void col_expo_kernel(const T* __restrict__ src, long long sstride, in
   if (lane == 0) expo[gw] = bound_expo(T(0), E);
 }
 
-// Left operand digits: out[b][s][c][r'] with r' < m the digits of Re A(r,c),
-// r' >= m those of Im A(r,c); A = src or src^H.  32 x 32 tiles through shared
+// Left operand digits: out[b][s][c][r'] (kp columns of 2 mp rows, the
+// padding zero) with r' < mp the digits of Re A(r,c), r' >= mp those of
+// Im A(r,c); A = src or src^H.  32 x 32 tiles through shared
 // memory so that reads and writes both coalesce.
 template <class T>
 __global__ void __launch_bounds__(256) slice_left_kernel(const T* __restrict__ src, long long sstride,
-                                                         int ld, bool conj, int m, int k,
+                                                         int ld, bool conj, int m, int k, int mp, int kp,
                                                          const int* __restrict__ ea, int na, int beta,
                                                          __nv_bfloat16* __restrict__ out) {
   __shared__ T tre[32][33], tim[32][33];
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(256) slice_left_kernel(const T* __restrict__ s
   __syncthreads();
   const int W = na * beta;
   const unsigned long long mask = (1ULL << beta) - 1ULL;
-  const size_t slice = (size_t)k * 2 * m;
+  const size_t slice = (size_t)kp * 2 * mp;
   for (int j = ty; j < 32; j += 8) {
     const int r = r0 + tx, c = c0 + j;
     if (r >= m || c >= k) continue;
@@ -136,26 +137,27 @@ __global__ void __launch_bounds__(256) slice_left_kernel(const T* __restrict__ s
     const int e = ea[(size_t)b * m + r];
     const unsigned long long Nr = fixed_bits(xr, e, W), Ni = fixed_bits(xi, e, W);
     const bool sr = xr < T(0), si = xi < T(0);
-    __nv_bfloat16* o = out + ((size_t)b * na * k + c) * 2 * m;
+    __nv_bfloat16* o = out + ((size_t)b * na * kp + c) * 2 * mp;
     for (int d = 0; d < na; ++d) {
       const int sh = W - beta * (d + 1);
       const int dr = (int)((Nr >> sh) & mask), di = (int)((Ni >> sh) & mask);
       o[(size_t)d * slice + r] = __float2bfloat16_rn((float)(sr ? -dr : dr));
-      o[(size_t)d * slice + r + m] = __float2bfloat16_rn((float)(si ? -di : di));
+      o[(size_t)d * slice + r + mp] = __float2bfloat16_rn((float)(si ? -di : di));
     }
   }
 }
 
-// Right operand digits: out[b][c'][row], c' < n the digits of Re B(r,c),
-// c' >= n those of Im B(r,c); digit t at rows (nbs-1-t)*k + r (ld nbs*k).
+// Right operand digits: out[b][c'][row] (2 np columns, the padding zero),
+// c' < np the digits of Re B(r,c), c' >= np those of Im B(r,c); digit t at
+// rows (nbs-1-t)*kp + r (ld nbs*kp).
 template <class T>
 __global__ void slice_right_kernel(const T* __restrict__ src, long long sstride, int ld, int k,
-                                   int n, const int* __restrict__ fb, int nbs, int beta, int nb,
-                                   __nv_bfloat16* __restrict__ out) {
+                                   int n, int kp, int np, const int* __restrict__ fb, int nbs,
+                                   int beta, int nb, __nv_bfloat16* __restrict__ out) {
   const size_t per = (size_t)k * n, total = per * nb;
   const int W = nbs * beta;
   const unsigned long long mask = (1ULL << beta) - 1ULL;
-  const size_t ldo = (size_t)nbs * k;
+  const size_t ldo = (size_t)nbs * kp;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
     const int b = (int)(idx / per);
@@ -166,32 +168,32 @@ __global__ void slice_right_kernel(const T* __restrict__ src, long long sstride,
     const int e = fb[(size_t)b * n + c];
     const unsigned long long Nr = fixed_bits(xr, e, W), Ni = fixed_bits(xi, e, W);
     const bool sr = xr < T(0), si = xi < T(0);
-    __nv_bfloat16* o = out + (size_t)b * 2 * n * ldo;
+    __nv_bfloat16* o = out + (size_t)b * 2 * np * ldo;
     for (int t = 0; t < nbs; ++t) {
       const int sh = W - beta * (t + 1);
       const int dr = (int)((Nr >> sh) & mask), di = (int)((Ni >> sh) & mask);
-      const size_t row = (size_t)(nbs - 1 - t) * k + r;
+      const size_t row = (size_t)(nbs - 1 - t) * kp + r;
       o[(size_t)c * ldo + row] = __float2bfloat16_rn((float)(sr ? -dr : dr));
-      o[(size_t)(c + n) * ldo + row] = __float2bfloat16_rn((float)(si ? -di : di));
+      o[(size_t)(c + np) * ldo + row] = __float2bfloat16_rn((float)(si ? -di : di));
     }
   }
 }
 
-// Combine the group products: G[d][b] is the 2m x 2n FP32 product of group d
+// Combine the group products: G[d][b] is the 2mp x 2np FP32 product of group d
 // (exact integers).  Group values (int32, exact) are added in 64-bit fixed
 // point, `per_acc` groups per accumulator; the accumulators are combined in
 // FP64 and scaled by 2^(e_r + f_c - 2 beta).
 __global__ void combine_kernel(const float* __restrict__ G, int ngroups, size_t gstride,
                                const int* __restrict__ ea, const int* __restrict__ fb, int m, int n,
-                               int beta, int per_acc, int nb, double* __restrict__ C) {
+                               int mp, int np, int beta, int per_acc, int nb, double* __restrict__ C) {
   const size_t per = (size_t)m * n, total = per * nb;
-  const size_t m2 = 2 * (size_t)m;
+  const size_t m2 = 2 * (size_t)mp;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
     const int b = (int)(idx / per);
     const size_t q = idx % per;
     const int r = (int)(q % m), c = (int)(q / m);
-    const float* g = G + (size_t)b * 4 * per;
+    const float* g = G + (size_t)b * 4 * mp * np;
     double accr = 0.0, acci = 0.0;
     for (int d0 = 0; d0 < ngroups; d0 += per_acc) {
       const int d1 = min(ngroups, d0 + per_acc);
@@ -199,9 +201,9 @@ __global__ void combine_kernel(const float* __restrict__ G, int ngroups, size_t 
       for (int d = d0; d < d1; ++d) {
         const float* gd = g + (size_t)d * gstride;
         const int rr = __float2int_rn(gd[(size_t)c * m2 + r]);
-        const int ii = __float2int_rn(gd[(size_t)(c + n) * m2 + r + m]);
-        const int ri = __float2int_rn(gd[(size_t)(c + n) * m2 + r]);
-        const int ir = __float2int_rn(gd[(size_t)c * m2 + r + m]);
+        const int ii = __float2int_rn(gd[(size_t)(c + np) * m2 + r + mp]);
+        const int ri = __float2int_rn(gd[(size_t)(c + np) * m2 + r]);
+        const int ir = __float2int_rn(gd[(size_t)c * m2 + r + mp]);
         ar = (ar << beta) + (long long)(rr - ii);
         ai = (ai << beta) + (long long)(ri + ir);
       }
@@ -244,15 +246,20 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
   const int ngroups = na + nbs - 1;
   // fixed-point accumulators: (int32 group values < 2^25) << beta * groups <= 2^62
   const int per_acc = std::max(1, (62 - 26 - 3) / beta + 1);
+  // GEMM dimensions padded to multiples of 8 (16-byte aligned BF16 rows and
+  // FP32 output columns); the padding digits are zero
+  const int mp = (m + 7) & ~7, np = (n + 7) & ~7, kp = (k + 7) & ~7;
+  const bool padded = mp != m || np != n || kp != k;
   // batch chunk so that the group products stay below ~8 GB
-  const size_t gbytes = (size_t)ngroups * 16 * (size_t)m * n;
+  const size_t gbytes = (size_t)ngroups * 16 * (size_t)mp * np;
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>(nb, (8ULL << 30) / std::max<size_t>(gbytes, 1)));
   __nv_bfloat16 *wa = nullptr, *wb = nullptr;
   float* G = nullptr;
   int *ea = nullptr, *fb = nullptr;
   int s;
-  if ((s = cuda_check(cudaMallocAsync((void**)&wa, 2ULL * chunk * na * k * 2 * m, st), "malloc digits A"))) return s;
-  if ((s = cuda_check(cudaMallocAsync((void**)&wb, 2ULL * chunk * 2 * n * nbs * k, st), "malloc digits B"))) return s;
+  const size_t abytes = 2ULL * chunk * na * kp * 2 * mp, bbytes = 2ULL * chunk * 2 * np * nbs * kp;
+  if ((s = cuda_check(cudaMallocAsync((void**)&wa, abytes, st), "malloc digits A"))) return s;
+  if ((s = cuda_check(cudaMallocAsync((void**)&wb, bbytes, st), "malloc digits B"))) return s;
   if ((s = cuda_check(cudaMallocAsync((void**)&G, gbytes * chunk, st), "malloc group products"))) return s;
   if ((s = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * chunk * m, st), "malloc ea"))) return s;
   if ((s = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * chunk * n, st), "malloc fb"))) return s;
@@ -262,27 +269,32 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
     const int cb = std::min(chunk, nb - b0);
     const TA* Ab = A + (size_t)b0 * sA;
     const TB* Bb = B + (size_t)b0 * sB;
+    if (padded) {
+      if ((s = cuda_check(cudaMemsetAsync(wa, 0, abytes, st), "clear digits A"))) return s;
+      if ((s = cuda_check(cudaMemsetAsync(wb, 0, bbytes, st), "clear digits B"))) return s;
+    }
     if (conjA) col_expo_kernel<TA><<<(int)(((size_t)m * cb * 32 + 255) / 256), 256, 0, st>>>(Ab, sA, lda, k, m, cb, ea);
     else row_expo_kernel<TA><<<(int)(((size_t)m * cb + 255) / 256), 256, 0, st>>>(Ab, sA, lda, m, k, cb, ea);
     col_expo_kernel<TB><<<(int)(((size_t)n * cb * 32 + 255) / 256), 256, 0, st>>>(Bb, sB, ldb, k, n, cb, fb);
     slice_left_kernel<TA><<<dim3((m + 31) / 32, (k + 31) / 32, cb), dim3(32, 8), 0, st>>>(
-        Ab, sA, lda, conjA, m, k, ea, na, beta, wa);
-    slice_right_kernel<TB><<<grid_of((size_t)k * n * cb), 256, 0, st>>>(Bb, sB, ldb, k, n, fb, nbs, beta, cb, wb);
+        Ab, sA, lda, conjA, m, k, mp, kp, ea, na, beta, wa);
+    slice_right_kernel<TB><<<grid_of((size_t)k * n * cb), 256, 0, st>>>(Bb, sB, ldb, k, n, kp, np, fb, nbs, beta,
+                                                                       cb, wb);
     scope.add_launches(4);
-    const size_t gstride = (size_t)cb * 4 * m * n;
+    const size_t gstride = (size_t)cb * 4 * mp * np;
     for (int d = 0; d < ngroups; ++d) {
       const int s_lo = std::max(0, d - (nbs - 1)), s_hi = std::min(na - 1, d);
       const int t_hi = d - s_lo;
       const int pairs = s_hi - s_lo + 1;
       cublasStatus_t bs = cublasGemmStridedBatchedEx(
-          ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * m, 2 * n, pairs * k, &one,
-          wa + (size_t)s_lo * k * 2 * m, CUDA_R_16BF, 2 * m, (long long)na * k * 2 * m,
-          wb + (size_t)(nbs - 1 - t_hi) * k, CUDA_R_16BF, nbs * k, (long long)2 * n * nbs * k, &zero,
-          G + (size_t)d * gstride, CUDA_R_32F, 2 * m, 4LL * m * n, cb, CUBLAS_COMPUTE_32F,
+          ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * mp, 2 * np, pairs * kp, &one,
+          wa + (size_t)s_lo * kp * 2 * mp, CUDA_R_16BF, 2 * mp, (long long)na * kp * 2 * mp,
+          wb + (size_t)(nbs - 1 - t_hi) * kp, CUDA_R_16BF, nbs * kp, (long long)2 * np * nbs * kp, &zero,
+          G + (size_t)d * gstride, CUDA_R_32F, 2 * mp, 4LL * mp * np, cb, CUBLAS_COMPUTE_32F,
           CUBLAS_GEMM_DEFAULT);
       if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "BF16 digit GEMM failed");
     }
-    combine_kernel<<<grid_of((size_t)m * n * cb), 256, 0, st>>>(G, ngroups, gstride, ea, fb, m, n, beta,
+    combine_kernel<<<grid_of((size_t)m * n * cb), 256, 0, st>>>(G, ngroups, gstride, ea, fb, m, n, mp, np, beta,
                                                                per_acc, cb, C + 2 * (size_t)b0 * m * n);
     scope.add_launches(1);
   }

@@ -102,22 +102,11 @@ __device__ __forceinline__ void block_sum2_d(double& a, double& b, double* red) 
 // cluster barriers per step.
 constexpr int kTrdPanel = 8;      // owned columns per warp and pass
 
-__device__ __forceinline__ void trd_element(float2& a, float2 vp, float2 wp, float2 vc, float2 cw,
-                                            float2 cv, bool pend, float& ax, float& ay) {
-  if (pend) {
-    const float2 t1 = cmul(vp, cw), t2 = cmul(wp, cv);
-    a.x -= t1.x + t2.x;
-    a.y -= t1.y + t2.y;
-  }
-  ax += a.x * vc.x + a.y * vc.y;       // conj(a) v
-  ay += a.x * vc.y - a.y * vc.x;
-}
-
 // One row pair (2q, 2q+1) of a panel: pending update, write-back, column
 // products and the pair's mirrored products.  MASK: the pair may lie on or
 // above a panel column's diagonal.
 template <bool PEND, bool MASK>
-__device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int q,
+__device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int ld, int q,
                                          const int (&cr)[kTrdPanel], const float2* __restrict__ vP,
                                          const float2* __restrict__ wP, const float2 (&vr)[kTrdPanel],
                                          float (&ax)[kTrdPanel], float (&ay)[kTrdPanel],
@@ -128,7 +117,7 @@ __device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int q,
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t)
     a4[t] = (cr[t] < n && (!MASK || cr[t] <= c0 + 1))
-                ? reinterpret_cast<const float4*>(Ak + (size_t)cr[t] * n)[q]
+                ? reinterpret_cast<const float4*>(Ak + (size_t)cr[t] * ld)[q]
                 : make_float4(0.f, 0.f, 0.f, 0.f);
   const float4 vc = vC4[q];
   float4 vp = make_float4(0.f, 0.f, 0.f, 0.f), wp = vp;
@@ -153,7 +142,7 @@ __device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int q,
     }
     ax[t] += a1.x * vc.z + a1.y * vc.w;
     ay[t] += a1.x * vc.w - a1.y * vc.z;
-    float2* colt = Ak + (size_t)cr[t] * n;
+    float2* colt = Ak + (size_t)cr[t] * ld;
     if (PEND) {
       if (m0) reinterpret_cast<float4*>(colt)[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
       else colt[c0 + 1] = a1;
@@ -180,7 +169,7 @@ __device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int q,
 // One panel of kTrdPanel owned columns (slots past the last column are
 // empty): the pairs touching the diagonals first, then the bulk unmasked.
 template <bool PEND>
-__device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int r0, int G, int pn, int nown,
+__device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld, int r0, int G, int pn, int nown,
                                           int lane, const float2* vP, const float2* wP, const float2* vC,
                                           float2* wC) {
   int cr[kTrdPanel];
@@ -200,11 +189,11 @@ __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int r0
   const float4* vP4 = reinterpret_cast<const float4*>(vP);
   const float4* wP4 = reinterpret_cast<const float4*>(wP);
   const float4* vC4 = reinterpret_cast<const float4*>(vC);
-  const int q1 = n >> 1;
+  const int q1 = ld >> 1;                       // the last pair may hold the zero padding row
   const int qd = min(q1, (c_last >> 1) + 1);    // pairs from qd on lie below every diagonal
   int q = (cr[0] >> 1) + lane;
-  for (; q < qd; q += 32) trd_pair<PEND, true>(Ak, n, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
-  for (; q < q1; q += 32) trd_pair<PEND, false>(Ak, n, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+  for (; q < qd; q += 32) trd_pair<PEND, true>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+  for (; q < q1; q += 32) trd_pair<PEND, false>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
     float x = ax[t], y = ay[t];
@@ -219,8 +208,7 @@ __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int r0
   }
 }
 
-template <bool VEC>
-__global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__ A, int n,
+__global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__ A, int n, int ld,
                                                             double* __restrict__ dout,
                                                             double* __restrict__ eout,
                                                             float2* __restrict__ tout) {
@@ -229,28 +217,28 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
   const int rank = (int)cl.block_rank();
   const int k = blockIdx.y;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  float2* Ak = A + (size_t)k * n * n;
+  float2* Ak = A + (size_t)k * n * ld;
   extern __shared__ float4 trd_sm4[];
   float2* trd_sm = reinterpret_cast<float2*>(trd_sm4);
   __shared__ double red[72];
   __shared__ float2 s_tau, s_scale;
   __shared__ float s_diag, s_beta;
   __shared__ double2 s_dot[16];
-  for (int e = tid; e < 4 * n; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
+  for (int e = tid; e < 4 * ld; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
   __syncthreads();
   cl.sync();
   int cur = 0;
   bool pend = false;
   for (int i = 0; i < n - 1; ++i) {
-    float2* vC = trd_sm + (size_t)(2 * cur) * n;        // v_i
-    float2* wC = trd_sm + (size_t)(2 * cur + 1) * n;    // partial A v_i, then w_i
-    const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;   // pending v_{i-1}
-    float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;     // pending w_{i-1}
+    float2* vC = trd_sm + (size_t)(2 * cur) * ld;        // v_i
+    float2* wC = trd_sm + (size_t)(2 * cur + 1) * ld;    // partial A v_i, then w_i
+    const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * ld;   // pending v_{i-1}
+    float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;     // pending w_{i-1}
     // ---- (a) every CTA: pending update of column i, reflector of column i ----
     // (column i is read from L2 by all CTAs; its owner writes v_i back only
     // after the next cluster barrier)
     {
-      const float2* col = Ak + (size_t)i * n;
+      const float2* col = Ak + (size_t)i * ld;
       float2 cw = make_float2(0.f, 0.f), cv = cw;
       if (pend) { cw = conjf2(wP[i]); cv = conjf2(vP[i]); }
       double part = 0.0;
@@ -291,40 +279,15 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
     const float2 tau = s_tau;
     int r0 = i + 1;
     r0 += ((rank - r0) % G + G) % G;
-    if (VEC) {
+    {
       // panels of kTrdPanel owned columns per warp; lane-owned row pairs
       // (2q, 2q+1) collect the mirrored products of the whole panel in
       // registers before one shared-memory atomic
       const int nown = r0 < n ? (n - r0 + G - 1) / G : 0;
       const int npanel = (nown + kTrdPanel - 1) / kTrdPanel;
       for (int pn = warp; pn < npanel; pn += nwarps) {
-        if (pend) trd_panel<true>(Ak, n, r0, G, pn, nown, lane, vP, wP, vC, wC);
-        else trd_panel<false>(Ak, n, r0, G, pn, nown, lane, vP, wP, vC, wC);
-      }
-    } else {
-      for (int r = r0 + warp * G; r < n; r += nwarps * G) {
-        float2* col = Ak + (size_t)r * n;
-        float2 cw = make_float2(0.f, 0.f), cv = cw;
-        if (pend) { cw = conjf2(wP[r]); cv = conjf2(vP[r]); }
-        const float2 vr = vC[r];
-        float ax = 0.f, ay = 0.f;
-        for (int c = r + lane; c < n; c += 32) {
-          float2 a = col[c];
-          trd_element(a, vP[c], wP[c], vC[c], cw, cv, pend, ax, ay);
-          if (pend) col[c] = a;
-          if (c > r) {
-            atomicAdd(&wC[c].x, a.x * vr.x - a.y * vr.y);
-            atomicAdd(&wC[c].y, a.x * vr.y + a.y * vr.x);
-          }
-        }
-        for (int o = 16; o; o >>= 1) {
-          ax += __shfl_xor_sync(0xffffffffu, ax, o);
-          ay += __shfl_xor_sync(0xffffffffu, ay, o);
-        }
-        if (lane == 0) {
-          atomicAdd(&wC[r].x, ax);
-          atomicAdd(&wC[r].y, ay);
-        }
+        if (pend) trd_panel<true>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, wC);
+        else trd_panel<false>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, wC);
       }
     }
     __syncthreads();
@@ -366,7 +329,7 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
       // the owner stores the reflector and T's entries
       if (rank == i % G) {
-        float2* col = Ak + (size_t)i * n;
+        float2* col = Ak + (size_t)i * ld;
         for (int r = i + 1 + tid; r < n; r += blockDim.x) col[r] = vC[r];
         if (tid == 0) {
           dout[(size_t)k * n + i] = s_diag;
@@ -382,10 +345,10 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
   // last diagonal element after the final pending update
   const int last = n - 1;
   if (rank == last % G && tid == 0) {
-    float2 a = Ak[(size_t)last * n + last];
+    float2 a = Ak[(size_t)last * ld + last];
     if (pend) {
-      const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * n;
-      const float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * n;
+      const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * ld;
+      const float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;
       const float2 t1 = cmul(vP[last], conjf2(wP[last])), t2 = cmul(wP[last], conjf2(vP[last]));
       a.x -= t1.x + t2.x;
     }
@@ -550,7 +513,7 @@ __global__ void invit_kernel(const double* __restrict__ d, const double* __restr
 // lists the groups, one warp per group.  Writes the result as complex FP32
 // columns into Zc [nk][n][n].
 __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict__ lam,
-                                                        double* __restrict__ Z, int n, double tol,
+                                                        double* __restrict__ Z, int n, int ld, double tol,
                                                         float2* __restrict__ Zc) {
   extern __shared__ int gstart[];
   __shared__ int ng;
@@ -594,8 +557,11 @@ __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict
     }
   }
   __syncthreads();
-  float2* Zck = Zc + (size_t)k * n * n;
-  for (size_t e = tid; e < (size_t)n * n; e += blockDim.x) Zck[e] = make_float2((float)Zk[e], 0.f);
+  float2* Zck = Zc + (size_t)k * n * ld;
+  for (size_t e = tid; e < (size_t)n * ld; e += blockDim.x) {
+    const int r = (int)(e % ld), c = (int)(e / ld);
+    Zck[e] = make_float2(r < n ? (float)Zk[(size_t)c * n + r] : 0.f, 0.f);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -605,7 +571,7 @@ __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict
 // rows above each reflector's leading 1 are zero, so that with j0 and n even
 // every GEMM operand starts on a 16-byte boundary).  V: [nk][nb][L] complex,
 // column-major.
-__global__ void build_v_kernel(const float2* __restrict__ A, int n, int j0, int nb, int L,
+__global__ void build_v_kernel(const float2* __restrict__ A, int n, int ld, int j0, int nb, int L,
                                int nk, float2* __restrict__ V) {
   const size_t total = (size_t)nk * nb * L;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
@@ -614,7 +580,7 @@ __global__ void build_v_kernel(const float2* __restrict__ A, int n, int j0, int 
     const int tcol = (int)((e / L) % nb);
     const int k = (int)(e / ((size_t)L * nb));
     const int r = j0 + rr, j = j0 + tcol;
-    V[e] = (r >= j + 1) ? A[(size_t)k * n * n + (size_t)j * n + r] : make_float2(0.f, 0.f);
+    V[e] = (r >= j + 1 && r < n) ? A[(size_t)k * n * ld + (size_t)j * ld + r] : make_float2(0.f, 0.f);
   }
 }
 
@@ -646,6 +612,19 @@ __global__ void tfactor_kernel(const float2* __restrict__ Gm, const float2* __re
   }
 }
 
+// [nk] matrices of n columns: leading dimension ld_in -> ld_out (rows
+// beyond n zero).
+__global__ void relayout_kernel(const float2* __restrict__ in, int n, int ld_in, int ld_out, int nk,
+                                float2* __restrict__ out) {
+  const size_t total = (size_t)nk * n * ld_out;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e % ld_out);
+    const size_t cb = e / ld_out;             // k * n + column
+    out[e] = r < n ? in[cb * ld_in + r] : make_float2(0.f, 0.f);
+  }
+}
+
 __global__ void ptr_array_kernel(float2* base, size_t stride, int nk, float2** out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < nk) out[k] = base + (size_t)k * stride;
@@ -665,13 +644,27 @@ int hetrd_max_n() {
 // reflectors; Cholesky factor).  ctx->d_info receives potrf's info per k.
 int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X) {
   cudaStream_t stream = ctx->stream;
-  const size_t nn = (size_t)n * n;
   int st;
   if (n < 2) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver needs n >= 2");
   if (n > hetrd_max_n()) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver: n above the shared-memory limit");
-  auto* H = reinterpret_cast<float2*>(h32);
-  auto* Sm = reinterpret_cast<float2*>(s32);
-  auto* Xc = reinterpret_cast<float2*>(X);
+  // columns padded to an even length (a zero row) so that every column
+  // starts on a 16-byte boundary; nn = batch stride
+  const int ld = n + (n & 1);
+  const size_t nn = (size_t)n * ld;
+  float2 *H = reinterpret_cast<float2*>(h32), *Sm = reinterpret_cast<float2*>(s32);
+  float2* Xc = reinterpret_cast<float2*>(X);
+  if (ld != n) {
+    float2 *Hq = nullptr, *Sq = nullptr, *Xq = nullptr;
+    if ((st = cuda_check(cudaMallocAsync((void**)&Hq, 8 * nn * nk, stream), "malloc padded H"))) return st;
+    if ((st = cuda_check(cudaMallocAsync((void**)&Sq, 8 * nn * nk, stream), "malloc padded S"))) return st;
+    if ((st = cuda_check(cudaMallocAsync((void**)&Xq, 8 * nn * nk, stream), "malloc padded X"))) return st;
+    relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, n, ld, nk, Hq);
+    relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(Sm, n, n, ld, nk, Sq);
+    count_launch(2);
+    H = Hq;
+    Sm = Sq;
+    Xc = Xq;
+  }
   float2** ptrs = nullptr;
   if ((st = cuda_check(cudaMallocAsync((void**)&ptrs, sizeof(float2*) * 3 * nk, stream), "malloc ptrs"))) return st;
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Sm, nn, nk, ptrs);
@@ -687,14 +680,14 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
     cusolverDnSetStream(ctx->solver, stream);
     if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
-    if (cusolverDnCpotrfBatched(ctx->solver, CUBLAS_FILL_MODE_UPPER, n, Sp, n, ctx->d_info, nk) !=
+    if (cusolverDnCpotrfBatched(ctx->solver, CUBLAS_FILL_MODE_UPPER, n, Sp, ld, ctx->d_info, nk) !=
         CUSOLVER_STATUS_SUCCESS)
       return fail(OLC_ERR_CUDA, "cusolverDnCpotrfBatched failed");
     if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, n, Hp, n, nk) != CUBLAS_STATUS_SUCCESS)
+                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Hp, ld, nk) != CUBLAS_STATUS_SUCCESS)
       return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-H H) failed");
     if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, n, Hp, n, nk) != CUBLAS_STATUS_SUCCESS)
+                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Hp, ld, nk) != CUBLAS_STATUS_SUCCESS)
       return fail(OLC_ERR_CUDA, "ctrsmBatched (H U^-1) failed");
   }
   // ---- 2. tridiagonalisation ----------------------------------------------
@@ -713,8 +706,8 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
       const int g = std::atoi(v);
       if (g == 1 || g == 2 || g == 4 || g == 8) G = g;
     }
-    const size_t smem = 4 * sizeof(float2) * (size_t)n;
-    auto kern = (n % 2 == 0) ? hetrd_kernel<true> : hetrd_kernel<false>;
+    const size_t smem = 4 * sizeof(float2) * (size_t)ld;
+    auto kern = hetrd_kernel;
     if ((st = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "hetrd smem"))) return st;
     cudaLaunchConfig_t cfg = {};
@@ -729,7 +722,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if ((st = cuda_check(cudaLaunchKernelEx(&cfg, kern, H, n, d, e, tau), "hetrd launch"))) return st;
+    if ((st = cuda_check(cudaLaunchKernelEx(&cfg, kern, H, n, ld, d, e, tau), "hetrd launch"))) return st;
   }
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
   const size_t T = (size_t)n * nk;
@@ -739,7 +732,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   if ((st = cuda_check(cudaMallocAsync((void**)&ef, 4ULL * T, stream), "malloc ef"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&work, 8ULL * 5 * n * T, stream), "malloc invit work"))) return st;
   if ((st = cuda_check(cudaMallocAsync((void**)&piv, (size_t)n * T, stream), "malloc piv"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&Z, 8ULL * nn * nk, stream), "malloc Z"))) return st;
+  if ((st = cuda_check(cudaMallocAsync((void**)&Z, 8ULL * n * n * nk, stream), "malloc Z"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
     tri_prep_kernel<<<(int)((T + 255) / 256), 256, 0, stream>>>(d, e, n, nk, df, ef);
@@ -748,7 +741,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     const size_t gsm = sizeof(int) * 2 * (size_t)(n / 2 + 1);
     if ((st = cuda_check(cudaFuncSetAttribute(group_mgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)gsm), "mgs smem"))) return st;
-    group_mgs_kernel<<<nk, 256, gsm, stream>>>(lam, Z, n, 1e-5, Xc);
+    group_mgs_kernel<<<nk, 256, gsm, stream>>>(lam, Z, n, ld, 1e-5, Xc);
   }
   cudaFreeAsync(work, stream);
   cudaFreeAsync(piv, stream);
@@ -776,19 +769,19 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
       const int nbb = std::min(kWyBlock, n - 1 - j0);
       const int L = n - j0;
       const long long sV = (long long)nbb * L, sG = (long long)nbb * nbb, sW = (long long)nbb * n;
-      build_v_kernel<<<std::min<size_t>((sV * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, j0, nbb, L, nk, V);
+      build_v_kernel<<<std::min<size_t>((sV * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, ld, j0, nbb, L, nk, V);
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
                                     &zero, Gc, nbb, sG, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H V failed");
       tfactor_kernel<<<nk, kWyBlock, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
-                                    Zx + j0, n, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
+                                    Zx + j0, ld, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm V^H Z failed");
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_N, CUBLAS_OP_N, nbb, n, nbb, &one, Tc, nbb, sG,
                                     W1c, nbb, sW, &zero, W2c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm T W failed");
       if (cublasCgemmStridedBatched(ctx->blas_f32, CUBLAS_OP_N, CUBLAS_OP_N, L, n, nbb, &mone, Vc, L, sV,
-                                    W2c, nbb, sW, &one, Zx + j0, n, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
+                                    W2c, nbb, sW, &one, Zx + j0, ld, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
         return fail(OLC_ERR_CUDA, "cgemm Z -= V W failed");
       scope.add_launches(2);
     }
@@ -802,8 +795,16 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
     if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, n, Xp, n, nk) != CUBLAS_STATUS_SUCCESS)
+                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Xp, ld, nk) != CUBLAS_STATUS_SUCCESS)
       return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-1 Z) failed");
+  }
+  if (ld != n) {
+    relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(
+        Xc, n, ld, n, nk, reinterpret_cast<float2*>(X));
+    count_launch();
+    cudaFreeAsync(H, stream);
+    cudaFreeAsync(Sm, stream);
+    cudaFreeAsync(Xc, stream);
   }
   cudaFreeAsync(d, stream);
   cudaFreeAsync(e, stream);

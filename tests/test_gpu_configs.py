@@ -1,0 +1,80 @@
+"""The workload configurations at (or near) their full sizes (gpu).
+
+* Diamond, 216 k-points (n = 8 or 10): every k against the oracle's
+  storage-form H(k), S(k) and LAPACK zhegv, eigenvalues within 1e-8 Ha.
+* Graphite (n = 32, valence only) on a slice of its 32x32x8 mesh: GPU
+  integrals and batched small solver against the oracle on sampled k.
+* Si8 (n = 104) on its full 8x8x8 mesh: mixed path against the FP64 path
+  (1e-6 Ha), FP64 path against the oracle on sampled k (1e-8 Ha).
+Properties that do not depend on size hold at every k: ascending order,
+S-orthonormal vectors.
+"""
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from olcao_gb300 import system as S
+
+EIG_TOL = 1e-8
+MIXED_EIG_TOL = 1e-6
+
+
+def _oracle_eigs(sysm, kidx):
+    part = S.System(**{**sysm.__dict__, "kpoints_abc": sysm.kpoints_abc[kidx]})
+    o = orc.Oracle(part)
+    packed = o.packed_operators()
+    w, _ = orc.zhegv(orc.assemble(packed, sysm.pot_coeffs), packed["S"], o.vale_dim, o.vale_dim)
+    return w
+
+
+@pytest.mark.gpu
+def test_diamond_all_kpoints_match_oracle(gpu_lib):
+    from olcao_gb300 import api
+    sysm = S.CONFIGS["diamond"]()
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n = ctx.vale_dim
+    assert ctx.nk == 216
+    w = ctx.scf_iteration(sysm.pot_coeffs, n)
+    ref = _oracle_eigs(sysm, np.arange(ctx.nk))
+    assert np.abs(w - ref).max() <= EIG_TOL
+    assert (np.diff(w, axis=1) >= 0).all()
+
+
+@pytest.mark.gpu
+def test_graphite_mesh_slice_matches_oracle(gpu_lib):
+    from olcao_gb300 import api
+    sysm = S.CONFIGS["graphite"]()
+    sysm.kpoints_abc = sysm.kpoints_abc[::16]          # 512 of the 8192 k-points
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n = ctx.vale_dim
+    assert n == 32
+    w = ctx.scf_iteration(sysm.pot_coeffs, n, precision=api.PREC_MIXED)
+    kidx = np.array([0, 101, 257, ctx.nk - 1])
+    ref = _oracle_eigs(sysm, kidx)
+    assert np.abs(w[kidx] - ref).max() <= EIG_TOL
+    assert (np.diff(w, axis=1) >= 0).all()
+
+
+@pytest.mark.gpu
+def test_si8_full_mesh_mixed_and_fp64(gpu_lib):
+    import torch
+    from olcao_gb300 import api
+    sysm = S.CONFIGS["si8"]()
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n, nk = ctx.vale_dim, ctx.nk
+    assert n == 104 and nk == 512
+    w64 = ctx.scf_iteration(sysm.pot_coeffs, n, precision=api.PREC_FP64)
+    vec = torch.zeros(nk, n, n, dtype=torch.complex128, device="cuda")
+    wm = ctx.scf_iteration(sysm.pot_coeffs, n, precision=api.PREC_MIXED, vectors=vec)
+    assert np.abs(wm - w64).max() <= MIXED_EIG_TOL
+    kidx = np.array([0, 333])
+    assert np.abs(w64[kidx] - _oracle_eigs(sysm, kidx)).max() <= EIG_TOL
+    X = vec.cpu().numpy()
+    for k in (0, 200, nk - 1):
+        _, Sm = ctx.scf_matrices(sysm.pot_coeffs, k)
+        Z = X[k].T
+        assert np.abs(Z.conj().T @ Sm @ Z - np.eye(n)).max() < 1e-4

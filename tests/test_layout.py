@@ -65,11 +65,9 @@ def test_setup_integrals_layout_matches_oracle(tmp_path, gpu_lib):
         for grp, key in names.items():
             d = api.read_dataset(root, f"/atomIntgGroup/{grp}/{kn}")
             assert d.shape == (2, plen)
-            ref = packed[key][k]
-            got = d[0] + 1j * d[1]
-            assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max() + 1e-14, (grp, k)
+            ref = packed[key][k].T          # oracle: [plen, (re, im)]
+            assert np.abs(d - ref).max() <= 1e-10 * np.abs(ref).max() + 1e-14, (grp, k)
         for j in range(o.pot_dim):
             d = api.read_dataset(root, f"/atomIntgGroup/atomPotOverlap/{kn}/{j + 1:07d}")
-            ref = packed[f"V{j}"][k]
-            got = d[0] + 1j * d[1]
-            assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max() + 1e-14, (j, k)
+            ref = packed[f"V{j}"][k].T
+            assert np.abs(d - ref).max() <= 1e-10 * np.abs(ref).max() + 1e-14, (j, k)
