@@ -58,25 +58,30 @@ int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32)
 // ---------------------------------------------------------------------------
 // extraction
 // ---------------------------------------------------------------------------
-constexpr int kMaxCluster = 64;     // states per exactly-solved cluster
-constexpr int kSmallCluster = 16;   // clusters up to this size use the small kernel
+constexpr int kMaxCluster = 64;     // states per exactly-solved block
+constexpr int kMaxCore = 48;        // core of a cluster cut out of a longer run
+constexpr int kBuffer = 8;          // neighbours solved with a cut core on each cut side
+constexpr int kSmallCluster = 16;   // blocks up to this size use the small kernel
 
 struct ClusterLists {
   int* order;      // [nk][n] state held by each sorted slot
   int* pos;        // [nk][n] sorted slot of each state
   double* diag;    // [nk][n] a_j = Hh_jj
   int* csize;      // [nk][n] size of the cluster holding each slot
-  int4* small;     // (k, first slot, size, 0): clusters of 2..kSmallCluster states
-  int4* large;     // clusters above kSmallCluster states
+  int4* small;     // (k, first slot, size, cut flags): blocks of up to kSmallCluster states
+  int4* large;     // larger blocks; flags bit 0 / 1: cut on the low / high side
   int* counters;   // [4] small count, large count, small next, large next
   int cap;         // capacity of each list
 };
 
 // Per k (one CTA): a_j = Re Hh_jj (the basis is orthonormal after the Loewdin
 // step), sorted ascending; clusters are runs of consecutive values closer than
-// kClusterGap.  A run longer than kMaxCluster is cut at its widest gap.  Fills
-// the per-k arrays of L and appends every cluster of two or more states to a
-// work list.
+// kClusterGap.  A run longer than kMaxCluster is cut into cores of at most
+// kMaxCore states at its widest gaps; a core is later solved together with
+// kBuffer neighbours on each cut side (only its own eigenpairs are kept), so
+// that the strongly coupled states across a cut are treated exactly.  Fills
+// the per-k arrays of L and appends every cluster except clean single states
+// to a work list.
 __global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict__ Hh, int n,
                                                        ClusterLists L) {
   extern __shared__ double sortmem[];
@@ -116,29 +121,38 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict_
     L.pos[(size_t)k * n + idx[i]] = i;
   }
   if (tid == 0) {
-    auto close = [&](int s0, int s1) {
+    // a cluster [s0, s1) with cut flags; clean singletons go to the warp kernel
+    auto close = [&](int s0, int s1, int flags) {
       const int m = s1 - s0;
-      for (int s = s0; s < s1; ++s) L.csize[(size_t)k * n + s] = m;
-      if (m > 1) {
-        const bool sm = m <= kSmallCluster;
+      for (int s = s0; s < s1; ++s) L.csize[(size_t)k * n + s] = flags ? -m : m;
+      if (m > 1 || flags) {
+        const int ext = m + ((flags & 1) ? min(kBuffer, s0) : 0) + ((flags & 2) ? min(kBuffer, n - s1) : 0);
+        const bool sm = ext <= kSmallCluster;
         const int at = atomicAdd(L.counters + (sm ? 0 : 1), 1);
-        if (at < L.cap) (sm ? L.small : L.large)[at] = make_int4(k, s0, m, 0);
+        if (at < L.cap) (sm ? L.small : L.large)[at] = make_int4(k, s0, m, flags);
       }
     };
-    int cur = 0;
+    int s0 = 0;
     for (int i = 1; i <= n; ++i) {
-      if (i == n || key[i] - key[i - 1] >= kClusterGap) {
-        close(cur, i);
-        cur = i;
-      } else if (i - cur >= kMaxCluster) {
-        // slots cur..i form a run of kMaxCluster + 1: end the cluster at the
-        // widest gap inside it
-        int g = cur + 1;
-        for (int t = cur + 2; t <= i; ++t)
-          if (key[t] - key[t - 1] > key[g] - key[g - 1]) g = t;
-        close(cur, g);
-        cur = g;
+      if (i < n && key[i] - key[i - 1] < kClusterGap) continue;
+      // run [s0, i) of values closer than kClusterGap
+      if (i - s0 <= kMaxCluster) {
+        close(s0, i, 0);
+      } else {
+        // cores of at most kMaxCore states, each ending at the widest gap
+        // it can reach; cut sides are solved with buffer states
+        int cur = s0, cutl = 0;
+        while (i - cur > kMaxCore) {
+          int g = cur + 1;
+          for (int t = cur + 2; t <= cur + kMaxCore; ++t)
+            if (key[t] - key[t - 1] > key[g] - key[g - 1]) g = t;
+          close(cur, g, cutl | 2);
+          cur = g;
+          cutl = 1;
+        }
+        close(cur, i, cutl);
       }
+      s0 = i;
     }
   }
 }
@@ -197,6 +211,7 @@ struct ClusterSmem {
   float2 Cp[32 * MAXM];      // [32][m] couplings A_jp of one chunk of j
   float w[32];               // 1 / (lc - a_j) of the chunk (0 inside the cluster)
   int cidx[MAXM];
+  int sel[MAXM];             // block eigenpair of each core slot
   float red[32];
   float off, fro;
   int item, rotated;
@@ -301,8 +316,9 @@ __device__ void jacobi_f32(ClusterSmem<MAXM>& S, int m) {
   }
 }
 
-// Clusters of two or more states, one work item per CTA at a time (items taken
-// from an atomic counter).  With lc the cluster's mean energy and
+// Clusters other than clean single states, one work item per CTA at a time
+// (items taken from an atomic counter); a cut core is extended by its buffer
+// states and keeps the eigenpairs ranked at its own positions.  With lc the cluster's mean energy and
 // F1 = sum_j A_.j A_j. / (lc - a_j), D2 = sum_j A_.j A_j. / (lc - a_j)^2 over
 // the states j outside the cluster, the folded pencil is
 //   (A - lc I + F1) y = (E - lc) (I + D2) y,
@@ -326,7 +342,11 @@ __global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float*
     const int item = S.item;
     if (item >= total) break;
     const int4 it = list[item];
-    const int k = it.x, s0 = it.y, m = it.z;
+    const int k = it.x, s0c = it.y, mc = it.z;
+    // the block: the core [s0c, s0c + mc) and buffer states on cut sides
+    const int bl = (it.w & 1) ? min(kBuffer, s0c) : 0;
+    const int br = (it.w & 2) ? min(kBuffer, n - s0c - mc) : 0;
+    const int s0 = s0c - bl, m = mc + bl + br;
     const double* H = Hh + 2 * (size_t)k * nn;
     const double* diag = L.diag + (size_t)k * n;
     const int* pos = L.pos + (size_t)k * n;
@@ -334,8 +354,8 @@ __global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float*
     __syncthreads();
     if (tid == 0) {
       double t = 0.0;
-      for (int p = 0; p < m; ++p) t += diag[S.cidx[p]];
-      S.lc = t / m;
+      for (int p = bl; p < bl + mc; ++p) t += diag[S.cidx[p]];
+      S.lc = t / mc;
     }
     __syncthreads();
     const double lc = S.lc;
@@ -413,11 +433,23 @@ __global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float*
     }
     __syncthreads();
     jacobi_f32<MAXM>(S, m);
-    // ---- eigenvalues: E = lc + mu (1 - z^H D2 z) ------------------------------
+    // ---- the core's eigenpairs: block eigenvalues ranked bl .. bl + mc - 1 ----
     for (int i = tid; i < m; i += blockDim.x) {
+      const float mi = S.C[i * m + i].x;
+      int rank = 0;
+      for (int j = 0; j < m; ++j) {
+        const float mj = S.C[j * m + j].x;
+        rank += (mj < mi) || (mj == mi && j < i);
+      }
+      if (rank >= bl && rank < bl + mc) S.sel[rank - bl] = i;
+    }
+    __syncthreads();
+    // ---- eigenvalues: E = lc + mu (1 - z^H D2 z) ------------------------------
+    for (int t = tid; t < mc; t += blockDim.x) {
+      const int i = S.sel[t];
       float dre = 0.f;
       for (int q = 0; q < m; ++q) {
-        float2 acc = make_float2(0.f, 0.f);      // (D2 z)_q... row q of D times z
+        float2 acc = make_float2(0.f, 0.f);      // (D2 z)_q
         for (int p = 0; p < m; ++p) {
           const float2 d = S.D[p * m + q], z = S.V[i * m + p];
           acc.x += d.x * z.x - d.y * z.y;
@@ -427,13 +459,13 @@ __global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float*
         dre += zq.x * acc.x + zq.y * acc.y;      // Re conj(z_q) (D z)_q
       }
       const double mu = S.C[i * m + i].x;
-      w_slot[(size_t)k * n + s0 + i] = lc + mu * (1.0 - (double)dre);
+      w_slot[(size_t)k * n + s0c + t] = lc + mu * (1.0 - (double)dre);
     }
     // ---- eigenvectors x_i = X z_i ---------------------------------------------
     if (v_slot) {
       const float2* Xk = reinterpret_cast<const float2*>(X) + (size_t)k * nn;
-      for (int i0 = 0; i0 < m; i0 += 8) {
-        const int I = min(8, m - i0);
+      for (int i0 = 0; i0 < mc; i0 += 8) {
+        const int I = min(8, mc - i0);
         for (int row = tid; row < n; row += blockDim.x) {
           float ar[8], ai[8];
 #pragma unroll
@@ -442,13 +474,13 @@ __global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float*
             const float2 xv = Xk[(size_t)S.cidx[p] * n + row];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-              const float2 z = S.V[min(i0 + b, m - 1) * m + p];
+              const float2 z = S.V[S.sel[min(i0 + b, mc - 1)] * m + p];
               ar[b] += xv.x * z.x - xv.y * z.y;
               ai[b] += xv.x * z.y + xv.y * z.x;
             }
           }
           for (int b = 0; b < I; ++b) {
-            double* o = v_slot + 2 * ((size_t)k * nn + (size_t)(s0 + i0 + b) * n + row);
+            double* o = v_slot + 2 * ((size_t)k * nn + (size_t)(s0c + i0 + b) * n + row);
             o[0] = ar[b];
             o[1] = ai[b];
           }
