@@ -247,11 +247,12 @@ int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num
 
 // FP64-accurate complex products from BF16 tensor-core digits (olc_ozaki.cu):
 // C[b] = op(A[b]) B[b], A logical m x k (conjA: A = src^H), B k x n, C m x n
-// complex FP64 with batch stride m*n; bits_a/bits_b = bits kept per operand.
+// complex FP64 with batch stride m*n; bits_a/bits_b = bits kept per operand;
+// batch strides sA, sB count elements of TA / TB (two per complex number).
 template <class TA, class TB>
 int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
-                int nb);
+                int nb, int stage = OLC_STAGE_REFINE);
 void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
 
 // raw layout-identical dataset writer (olc_layout.cu)

@@ -11,6 +11,7 @@
 // The GEMMs are FP64 complex library GEMMs (cuBLAS); the epilogue that
 // combines, flushes and packs is a hand-written kernel; the small-n solves
 // use a batched in-shared-memory kernel (olc_eigen_small.cu).
+#include <cstdlib>
 #include <algorithm>
 #include <cstdio>
 
@@ -165,7 +166,6 @@ int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const dou
                   const double* add) {
   const int nv = ctx->dims.vale_dim, nc = ctx->dims.core_dim, nk = ctx->dims.num_kpoints;
   int st;
-  StageScope scope(ctx, OLC_STAGE_ORTHO);
   if (nc) {
     const size_t nn = (size_t)nv * nv;
     if (!ctx->d_work_x) {
@@ -173,29 +173,20 @@ int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const dou
       if ((st = dalloc(ctx, &ctx->d_work_y, 2 * nn * nk))) return st;
       if ((st = dalloc(ctx, &ctx->d_work_w, 2 * (size_t)nv * nc * nk))) return st;
     }
-    const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0);
-    const cuDoubleComplex zero = make_cuDoubleComplex(0.0, 0.0);
-    const auto* S = reinterpret_cast<const cuDoubleComplex*>(scv);
-    const auto* O = reinterpret_cast<const cuDoubleComplex*>(cv);
-    const auto* CC = reinterpret_cast<const cuDoubleComplex*>(cc);
-    auto* X = reinterpret_cast<cuDoubleComplex*>(ctx->d_work_x);
-    auto* Y = reinterpret_cast<cuDoubleComplex*>(ctx->d_work_y);
-    auto* W = reinterpret_cast<cuDoubleComplex*>(ctx->d_work_w);
-    const long long sCV = (long long)nc * nv, sCC = (long long)nc * nc, sVV = (long long)nn,
-                    sW = (long long)nv * nc;
-    cublasStatus_t bs;
+    // the three products on the tensor cores, FP64-accurate (split digits,
+    // olc_ozaki.cu); OLC_ORTHO_BITS lowers the bits kept per operand
+    int bits = 53;
+    if (const char* v = std::getenv("OLC_ORTHO_BITS")) bits = std::max(24, std::min(53, std::atoi(v)));
+    const long long sCV = 2LL * nc * nv, sCC = 2LL * nc * nc, sW = 2LL * nv * nc;
     // X = S_cv^H O_cv
-    bs = cublasZgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nv, nv, nc, &one, S, nc,
-                                   sCV, is_overlap ? S : O, nc, sCV, &zero, X, nv, sVV, nk);
-    if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cublasZgemm (X) failed");
+    if ((st = ozaki_zgemm<double, double>(ctx, nv, nv, nc, scv, sCV, nc, true, bits, is_overlap ? scv : cv,
+                                          sCV, nc, bits, ctx->d_work_x, nk, OLC_STAGE_ORTHO))) return st;
     // W = S_cv^H O_cc
-    bs = cublasZgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nv, nc, nc, &one, S, nc,
-                                   sCV, CC, nc, sCC, &zero, W, nv, sW, nk);
-    if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cublasZgemm (W) failed");
+    if ((st = ozaki_zgemm<double, double>(ctx, nv, nc, nc, scv, sCV, nc, true, bits, cc, sCC, nc, bits,
+                                          ctx->d_work_w, nk, OLC_STAGE_ORTHO))) return st;
     // Y = W S_cv
-    bs = cublasZgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, nv, nv, nc, &one, W, nv,
-                                   sW, S, nc, sCV, &zero, Y, nv, sVV, nk);
-    if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cublasZgemm (Y) failed");
+    if ((st = ozaki_zgemm<double, double>(ctx, nv, nv, nc, ctx->d_work_w, sW, nv, false, bits, scv, sCV, nc,
+                                          bits, ctx->d_work_y, nk, OLC_STAGE_ORTHO))) return st;
   }
   PackArgs a;
   a.vv = vv;
@@ -209,6 +200,7 @@ int ortho_pack_ex(olc_context* ctx, bool is_overlap, const double* vv, const dou
   a.nc = nc;
   a.is_overlap = is_overlap ? 1 : 0;
   const size_t total = (size_t)nv * (nv + 1) / 2 * nk;
+  StageScope scope(ctx, OLC_STAGE_ORTHO);
   ortho_pack_kernel<<<grid_for(total), 256, 0, ctx->stream>>>(a);
   return cuda_check(cudaGetLastError(), "ortho_pack_kernel");
 }

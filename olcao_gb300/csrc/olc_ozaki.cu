@@ -239,7 +239,7 @@ void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs) {
 template <class TA, class TB>
 int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
-                int nb) {
+                int nb, int stage) {
   cudaStream_t st = ctx->stream;
   int beta, na, nbs;
   ozaki_plan(k, bits_a, bits_b, &beta, &na, &nbs);
@@ -263,7 +263,7 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
   if ((s = cuda_check(cudaMallocAsync((void**)&G, gbytes * chunk, st), "malloc group products"))) return s;
   if ((s = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * chunk * m, st), "malloc ea"))) return s;
   if ((s = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * chunk * n, st), "malloc fb"))) return s;
-  StageScope scope(ctx, OLC_STAGE_REFINE, 0);
+  StageScope scope(ctx, stage, 0);
   const float one = 1.0f, zero = 0.0f;
   for (int b0 = 0; b0 < nb; b0 += chunk) {
     const int cb = std::min(chunk, nb - b0);
@@ -307,10 +307,10 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
 }
 
 template int ozaki_zgemm<double, float>(olc_context*, int, int, int, const double*, long long, int, bool,
-                                        int, const float*, long long, int, int, double*, int);
+                                        int, const float*, long long, int, int, double*, int, int);
 template int ozaki_zgemm<float, double>(olc_context*, int, int, int, const float*, long long, int, bool,
-                                        int, const double*, long long, int, int, double*, int);
+                                        int, const double*, long long, int, int, double*, int, int);
 template int ozaki_zgemm<double, double>(olc_context*, int, int, int, const double*, long long, int, bool,
-                                         int, const double*, long long, int, int, double*, int);
+                                         int, const double*, long long, int, int, double*, int, int);
 
 }  // namespace olc
