@@ -182,39 +182,56 @@ __global__ void slice_right_kernel(const T* __restrict__ src, long long sstride,
 // Combine the group products: G[d][b] is the 2mp x 2np FP32 product of group d
 // (exact integers).  Group values (int32, exact) are added in 64-bit fixed
 // point, `per_acc` groups per accumulator; the accumulators are combined in
-// FP64 and scaled by 2^(e_r + f_c - 2 beta).
+// FP64 and scaled by 2^(e_r + f_c - 2 beta).  One thread per 4 consecutive
+// rows of one column (16-byte loads; mp is a multiple of 8).
 __global__ void combine_kernel(const float* __restrict__ G, int ngroups, size_t gstride,
                                const int* __restrict__ ea, const int* __restrict__ fb, int m, int n,
                                int mp, int np, int beta, int per_acc, int nb, double* __restrict__ C) {
-  const size_t per = (size_t)m * n, total = per * nb;
+  const int mq = (m + 3) >> 2;                 // row quads per column
+  const size_t per = (size_t)mq * n, total = per * nb;
   const size_t m2 = 2 * (size_t)mp;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
     const int b = (int)(idx / per);
     const size_t q = idx % per;
-    const int r = (int)(q % m), c = (int)(q / m);
+    const int r0 = 4 * (int)(q % mq), c = (int)(q / mq);
     const float* g = G + (size_t)b * 4 * mp * np;
-    double accr = 0.0, acci = 0.0;
+    double accr[4] = {0.0, 0.0, 0.0, 0.0}, acci[4] = {0.0, 0.0, 0.0, 0.0};
     for (int d0 = 0; d0 < ngroups; d0 += per_acc) {
       const int d1 = min(ngroups, d0 + per_acc);
-      long long ar = 0, ai = 0;
+      long long ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
       for (int d = d0; d < d1; ++d) {
         const float* gd = g + (size_t)d * gstride;
-        const int rr = __float2int_rn(gd[(size_t)c * m2 + r]);
-        const int ii = __float2int_rn(gd[(size_t)(c + np) * m2 + r + mp]);
-        const int ri = __float2int_rn(gd[(size_t)(c + np) * m2 + r]);
-        const int ir = __float2int_rn(gd[(size_t)c * m2 + r + mp]);
-        ar = (ar << beta) + (long long)(rr - ii);
-        ai = (ai << beta) + (long long)(ri + ir);
+        const float4 rr = *reinterpret_cast<const float4*>(gd + (size_t)c * m2 + r0);
+        const float4 ii = *reinterpret_cast<const float4*>(gd + (size_t)(c + np) * m2 + r0 + mp);
+        const float4 ri = *reinterpret_cast<const float4*>(gd + (size_t)(c + np) * m2 + r0);
+        const float4 ir = *reinterpret_cast<const float4*>(gd + (size_t)c * m2 + r0 + mp);
+        ar[0] = (ar[0] << beta) + (long long)(__float2int_rn(rr.x) - __float2int_rn(ii.x));
+        ar[1] = (ar[1] << beta) + (long long)(__float2int_rn(rr.y) - __float2int_rn(ii.y));
+        ar[2] = (ar[2] << beta) + (long long)(__float2int_rn(rr.z) - __float2int_rn(ii.z));
+        ar[3] = (ar[3] << beta) + (long long)(__float2int_rn(rr.w) - __float2int_rn(ii.w));
+        ai[0] = (ai[0] << beta) + (long long)(__float2int_rn(ri.x) + __float2int_rn(ir.x));
+        ai[1] = (ai[1] << beta) + (long long)(__float2int_rn(ri.y) + __float2int_rn(ir.y));
+        ai[2] = (ai[2] << beta) + (long long)(__float2int_rn(ri.z) + __float2int_rn(ir.z));
+        ai[3] = (ai[3] << beta) + (long long)(__float2int_rn(ri.w) + __float2int_rn(ir.w));
       }
       const double w = exp2_int(-beta * (d1 - 1));
-      accr = fma((double)ar, w, accr);
-      acci = fma((double)ai, w, acci);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        accr[u] = fma((double)ar[u], w, accr[u]);
+        acci[u] = fma((double)ai[u], w, acci[u]);
+      }
     }
-    const double sc = exp2_int(ea[(size_t)b * m + r] + fb[(size_t)b * n + c] - 2 * beta);
-    double* o = C + 2 * ((size_t)b * per + (size_t)c * m + r);
-    o[0] = accr * sc;
-    o[1] = acci * sc;
+    const int fc = fb[(size_t)b * n + c];
+    double* o = C + 2 * ((size_t)b * m * n + (size_t)c * m);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = r0 + u;
+      if (r >= m) break;
+      const double sc = exp2_int(ea[(size_t)b * m + r] + fc - 2 * beta);
+      o[2 * r] = accr[u] * sc;
+      o[2 * r + 1] = acci[u] * sc;
+    }
   }
 }
 
@@ -294,7 +311,7 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
           CUBLAS_GEMM_DEFAULT);
       if (bs != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "BF16 digit GEMM failed");
     }
-    combine_kernel<<<grid_of((size_t)m * n * cb), 256, 0, st>>>(G, ngroups, gstride, ea, fb, m, n, mp, np, beta,
+    combine_kernel<<<grid_of((size_t)((m + 3) / 4) * n * cb), 256, 0, st>>>(G, ngroups, gstride, ea, fb, m, n, mp, np, beta,
                                                                per_acc, cb, C + 2 * (size_t)b0 * m * n);
     scope.add_launches(1);
   }
