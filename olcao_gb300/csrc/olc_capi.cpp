@@ -127,6 +127,19 @@ int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
   }
   cublasSetStream(ctx->blas_f32, ctx->stream);
   {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess) {
+      ctx->pool = nullptr;
+      olc_destroy(ctx);
+      return fail(OLC_ERR_CUDA, "cudaMemPoolCreate failed");
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  {
     const char* v = std::getenv("OLC_FP32_GEMM");
     if (!(v && std::string(v) == "simt")) {
       cublasSetMathMode(ctx->blas_f32, CUBLAS_FP32_EMULATED_BF16X9_MATH);
@@ -171,6 +184,10 @@ int olc_destroy(olc_context_t* ctx) {
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->blas) cublasDestroy(ctx->blas);
   if (ctx->blas_f32) cublasDestroy(ctx->blas_f32);
+  if (ctx->pool) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaMemPoolDestroy(ctx->pool);
+  }
   if (ctx->solver) cusolverDnDestroy(ctx->solver);
   delete ctx;
   return OLC_OK;
@@ -200,7 +217,7 @@ int olc_gauss_overlap(olc_context_t* ctx, int op, int term, const double* coeffs
     const int pd = ctx->dims.pot_dim;
     std::vector<double> c(coeffs, coeffs + pd);
     double* dco = nullptr;
-    if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * std::max(1, pd), ctx->stream), "malloc"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&dco, sizeof(double) * std::max(1, pd), ctx->stream), "malloc"))) return st;
     cudaMemcpyAsync(dco, c.data(), sizeof(double) * pd, cudaMemcpyHostToDevice, ctx->stream);
     st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, precision, false);
     if (!st) st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, precision, true);

@@ -111,6 +111,7 @@ struct olc_context {
   cudaStream_t stream = nullptr;
   cublasHandle_t blas = nullptr;
   cublasHandle_t blas_f32 = nullptr;   // FP32 products (BF16x9 emulation)
+  cudaMemPool_t pool = nullptr;        // scratch of the SCF pass, kept between calls
   cusolverDnHandle_t solver = nullptr;
   // host copies
   olc_dims_t dims{};
@@ -171,6 +172,13 @@ struct olc_context {
 };
 
 namespace olc {
+
+// Stream-ordered scratch from the context's own pool: the pool keeps freed
+// memory (release threshold = max), so repeated SCF passes do not go back to
+// the driver for their tens of GB of scratch.
+inline cudaError_t ctx_malloc(olc_context* ctx, void** p, size_t bytes, cudaStream_t s) {
+  return ctx->pool ? cudaMallocFromPoolAsync(p, bytes, ctx->pool, s) : cudaMallocAsync(p, bytes, s);
+}
 
 void set_error(const std::string& msg);
 void count_launch(int n = 1);

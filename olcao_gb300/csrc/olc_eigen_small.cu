@@ -97,7 +97,7 @@ int solve_small_batched(olc_context* ctx, const double* h_full, const double* s_
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "smem attribute"))) return st;
   int32_t* dinfo = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&dinfo, sizeof(int32_t) * nk, ctx->stream), "malloc info"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dinfo, sizeof(int32_t) * nk, ctx->stream), "malloc info"))) return st;
   StageScope scope(ctx, OLC_STAGE_SOLVE);
   // OLC_SMALL_SOLVER_TRACE=1 prints each k-point's Jacobi convergence history
   double* dtrace = nullptr;

@@ -108,7 +108,7 @@ int write_setup_integrals(olc_context* ctx, const char* root) {
   if ((st = make_dirs(root))) return st;
   // overlap: pack the upper part of the orthogonalised S
   double* dS = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&dS, 8 * plen2, ctx->stream), "malloc packed S"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dS, 8 * plen2, ctx->stream), "malloc packed S"))) return st;
   pack_upper_kernel<<<(int)std::min<size_t>((plen * nk + 255) / 256, 152 * 16), 256, 0, ctx->stream>>>(
       ctx->d_chol, nv, nk, dS);
   count_launch();

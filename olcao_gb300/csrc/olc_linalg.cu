@@ -218,8 +218,8 @@ int assemble_packed(olc_context* ctx, const double* const* terms, const double* 
   const double** dterms = nullptr;
   double* dco = nullptr;
   int st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&dterms, sizeof(double*) * nterm, ctx->stream), "malloc"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * nterm, ctx->stream), "malloc"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dterms, sizeof(double*) * nterm, ctx->stream), "malloc"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dco, sizeof(double) * nterm, ctx->stream), "malloc"))) return st;
   cudaMemcpyAsync(dterms, terms, sizeof(double*) * nterm, cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(dco, coeffs, sizeof(double) * nterm, cudaMemcpyHostToDevice, ctx->stream);
   {
@@ -290,7 +290,7 @@ int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
   double* eig_dev = eigenvalues;
   double* tmp_eigs = nullptr;
   if (!eig_on_device) {
-    if ((st = cuda_check(cudaMallocAsync((void**)&tmp_eigs, sizeof(double) * (size_t)num_states * nk,
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&tmp_eigs, sizeof(double) * (size_t)num_states * nk,
                                          ctx->stream), "malloc eigs"))) return st;
     eig_dev = tmp_eigs;
   }
@@ -353,7 +353,7 @@ int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* e
     double* tmp = nullptr;
     const int nk = ctx->dims.num_kpoints;
     if (!eig_on_device) {
-      if ((st = cuda_check(cudaMallocAsync((void**)&tmp, sizeof(double) * (size_t)num_states * nk,
+      if ((st = cuda_check(ctx_malloc(ctx, (void**)&tmp, sizeof(double) * (size_t)num_states * nk,
                                            ctx->stream), "malloc eigs"))) return st;
       eig_dev = tmp;
     }
@@ -375,7 +375,7 @@ int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* e
     double* tmp = nullptr;
     const int nk = ctx->dims.num_kpoints;
     if (!eig_on_device) {
-      if ((st = cuda_check(cudaMallocAsync((void**)&tmp, sizeof(double) * (size_t)num_states * nk,
+      if ((st = cuda_check(ctx_malloc(ctx, (void**)&tmp, sizeof(double) * (size_t)num_states * nk,
                                            ctx->stream), "malloc eigs"))) return st;
       eig_dev = tmp;
     }
@@ -514,7 +514,7 @@ int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, 
   const size_t nn = (size_t)nv * nv;
   double* hall = nullptr;
   int st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&hall, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&hall, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
   st = build_hamiltonian(ctx, coeffs, ctx->prep_precision, 0, hall);
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   if (!st && h) st = cuda_check(cudaMemcpyAsync(h, hall + 2 * nn * kpoint, 16 * nn, kind, ctx->stream), "copy h");
@@ -532,8 +532,8 @@ int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num
   const size_t nn = (size_t)nv * nv;
   int st;
   double *h = nullptr, *s = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
   if ((st = build_hamiltonian(ctx, coeffs, precision, flags, h))) return st;
   cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
   st = solve_full(ctx, h, s, num_states, eigenvalues, (flags & OLC_ITER_EIG_DEVICE) ? 1 : 0,
@@ -552,7 +552,7 @@ int build_hamiltonian(olc_context* ctx, const double* coeffs, int precision, int
   // is exactly 0 unscaled (matrixSubs.F90:278-282)
   double* dco = nullptr;
   const int off = ctx->prep_form == OLC_FORM_STORED ? 2 : 0;
-  if ((st = cuda_check(cudaMallocAsync((void**)&dco, sizeof(double) * (pd + 2), ctx->stream), "malloc coeffs"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dco, sizeof(double) * (pd + 2), ctx->stream), "malloc coeffs"))) return st;
   if (flags & OLC_ITER_COEFF_DEVICE) {
     cudaMemcpyAsync(dco + off, coeffs, sizeof(double) * pd, cudaMemcpyDeviceToDevice, ctx->stream);
   } else {

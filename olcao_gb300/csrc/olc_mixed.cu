@@ -599,10 +599,10 @@ int loewdin(olc_context* ctx, int n, int nk, double* Hh, double* Sh, float* X) {
   const size_t nn = (size_t)n * n, total = nn * nk;
   float *E = nullptr, *F = nullptr, *H32 = nullptr, *T = nullptr;
   int st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&E, 8 * total, stream), "malloc E"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&F, 8 * total, stream), "malloc F"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&H32, 8 * total, stream), "malloc H32"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&T, 8 * total, stream), "malloc T"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&E, 8 * total, stream), "malloc E"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&F, 8 * total, stream), "malloc F"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&H32, 8 * total, stream), "malloc H32"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&T, 8 * total, stream), "malloc T"))) return st;
   StageScope scope(ctx, OLC_STAGE_REFINE, 0);
   loewdin_prep_kernel<<<grid_for(total), 256, 0, stream>>>(Hh, Sh, n, total, E, H32);
   const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
@@ -644,7 +644,7 @@ static int solve_fp32_library(olc_context* ctx, int n, int nk, float* h32, float
   cudaStream_t stream = ctx->stream;
   int st;
   float* w32 = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&w32, 4 * (size_t)n * nk, stream), "malloc w32"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&w32, 4 * (size_t)n * nk, stream), "malloc w32"))) return st;
   const int nsub = std::max(1, std::min(nk, 32));
   if ((int)ctx->mixed_streams.size() != nsub || ctx->mixed_n != n) {
     for (size_t i = 0; i < ctx->mixed_streams.size(); ++i) {
@@ -729,8 +729,8 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   cudaStream_t stream = ctx->stream;
   // ---- 1. FP32 generalised solve per k -----------------------------------
   float *h32 = nullptr, *s32 = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 2);
     to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
@@ -738,7 +738,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   }
   float* X = nullptr;      // FP32 eigenvectors, [nk][n][n] complex
   if (use_batched_fp32(n)) {
-    if ((st = cuda_check(cudaMallocAsync((void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
     if ((st = solve_fp32_batched(ctx, n, nk, h32, s32, X))) return st;
     cudaFreeAsync(h32, stream);
   } else {
@@ -752,9 +752,9 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   int b64 = 48;
   const int b32 = 24;
   if (const char* v = std::getenv("OLC_SPLIT_BITS")) b64 = std::max(24, std::min(53, std::atoi(v)));
-  if ((st = cuda_check(cudaMallocAsync((void**)&Y, 16ULL * nn * nk, stream), "malloc Y"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&Hh, 16ULL * nn * nk, stream), "malloc Hh"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&Sh, 16ULL * nn * nk, stream), "malloc Sh"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&Y, 16ULL * nn * nk, stream), "malloc Y"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&Hh, 16ULL * nn * nk, stream), "malloc Hh"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&Sh, 16ULL * nn * nk, stream), "malloc Sh"))) return st;
   const long long snn = (long long)nn * 2;
   // Y = H X ; Hh = X^H Y
   if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk))) return st;
@@ -771,15 +771,15 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   ClusterLists L{};
   L.cap = (n / 2 + 1) * nk;
   double *w_slot = nullptr, *v_slot = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.order, 4ULL * n * nk, stream), "malloc order"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.pos, 4ULL * n * nk, stream), "malloc pos"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.csize, 4ULL * n * nk, stream), "malloc csize"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.diag, 8ULL * n * nk, stream), "malloc diag"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.small, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.large, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&L.counters, 4 * sizeof(int), stream), "malloc counters"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&w_slot, 8ULL * n * nk, stream), "malloc w"))) return st;
-  if (vectors && (st = cuda_check(cudaMallocAsync((void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.order, 4ULL * n * nk, stream), "malloc order"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.pos, 4ULL * n * nk, stream), "malloc pos"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.csize, 4ULL * n * nk, stream), "malloc csize"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.diag, 8ULL * n * nk, stream), "malloc diag"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.small, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.large, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.counters, 4 * sizeof(int), stream), "malloc counters"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&w_slot, 8ULL * n * nk, stream), "malloc w"))) return st;
+  if (vectors && (st = cuda_check(ctx_malloc(ctx, (void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_REFINE, 4);
     int P = 1;

@@ -275,11 +275,11 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
   int *ea = nullptr, *fb = nullptr;
   int s;
   const size_t abytes = 2ULL * chunk * na * kp * 2 * mp, bbytes = 2ULL * chunk * 2 * np * nbs * kp;
-  if ((s = cuda_check(cudaMallocAsync((void**)&wa, abytes, st), "malloc digits A"))) return s;
-  if ((s = cuda_check(cudaMallocAsync((void**)&wb, bbytes, st), "malloc digits B"))) return s;
-  if ((s = cuda_check(cudaMallocAsync((void**)&G, gbytes * chunk, st), "malloc group products"))) return s;
-  if ((s = cuda_check(cudaMallocAsync((void**)&ea, 4ULL * chunk * m, st), "malloc ea"))) return s;
-  if ((s = cuda_check(cudaMallocAsync((void**)&fb, 4ULL * chunk * n, st), "malloc fb"))) return s;
+  if ((s = cuda_check(ctx_malloc(ctx, (void**)&wa, abytes, st), "malloc digits A"))) return s;
+  if ((s = cuda_check(ctx_malloc(ctx, (void**)&wb, bbytes, st), "malloc digits B"))) return s;
+  if ((s = cuda_check(ctx_malloc(ctx, (void**)&G, gbytes * chunk, st), "malloc group products"))) return s;
+  if ((s = cuda_check(ctx_malloc(ctx, (void**)&ea, 4ULL * chunk * m, st), "malloc ea"))) return s;
+  if ((s = cuda_check(ctx_malloc(ctx, (void**)&fb, 4ULL * chunk * n, st), "malloc fb"))) return s;
   StageScope scope(ctx, stage, 0);
   const float one = 1.0f, zero = 0.0f;
   for (int b0 = 0; b0 < nb; b0 += chunk) {

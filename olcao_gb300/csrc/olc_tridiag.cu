@@ -655,9 +655,9 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   float2* Xc = reinterpret_cast<float2*>(X);
   if (ld != n) {
     float2 *Hq = nullptr, *Sq = nullptr, *Xq = nullptr;
-    if ((st = cuda_check(cudaMallocAsync((void**)&Hq, 8 * nn * nk, stream), "malloc padded H"))) return st;
-    if ((st = cuda_check(cudaMallocAsync((void**)&Sq, 8 * nn * nk, stream), "malloc padded S"))) return st;
-    if ((st = cuda_check(cudaMallocAsync((void**)&Xq, 8 * nn * nk, stream), "malloc padded X"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Hq, 8 * nn * nk, stream), "malloc padded H"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Sq, 8 * nn * nk, stream), "malloc padded S"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Xq, 8 * nn * nk, stream), "malloc padded X"))) return st;
     relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, n, ld, nk, Hq);
     relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(Sm, n, n, ld, nk, Sq);
     count_launch(2);
@@ -666,7 +666,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     Xc = Xq;
   }
   float2** ptrs = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&ptrs, sizeof(float2*) * 3 * nk, stream), "malloc ptrs"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&ptrs, sizeof(float2*) * 3 * nk, stream), "malloc ptrs"))) return st;
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Sm, nn, nk, ptrs);
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(H, nn, nk, ptrs + nk);
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Xc, nn, nk, ptrs + 2 * nk);
@@ -694,9 +694,9 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   double *d = nullptr, *e = nullptr, *lam = nullptr, *work = nullptr, *Z = nullptr;
   float2* tau = nullptr;
   unsigned char* piv = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&d, 8ULL * n * nk, stream), "malloc d"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&e, 8ULL * (n - 1) * nk, stream), "malloc e"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&d, 8ULL * n * nk, stream), "malloc d"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&e, 8ULL * (n - 1) * nk, stream), "malloc e"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 1);
     // CTAs per k: enough clusters to fill the SMs (OLC_TRD_CLUSTER overrides)
@@ -726,13 +726,13 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   }
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
   const size_t T = (size_t)n * nk;
-  if ((st = cuda_check(cudaMallocAsync((void**)&lam, 8ULL * T, stream), "malloc lam"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&lam, 8ULL * T, stream), "malloc lam"))) return st;
   float *df = nullptr, *ef = nullptr;
-  if ((st = cuda_check(cudaMallocAsync((void**)&df, 4ULL * T, stream), "malloc df"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&ef, 4ULL * T, stream), "malloc ef"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&work, 8ULL * 5 * n * T, stream), "malloc invit work"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&piv, (size_t)n * T, stream), "malloc piv"))) return st;
-  if ((st = cuda_check(cudaMallocAsync((void**)&Z, 8ULL * n * n * nk, stream), "malloc Z"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&df, 4ULL * T, stream), "malloc df"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&ef, 4ULL * T, stream), "malloc ef"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&work, 8ULL * 5 * n * T, stream), "malloc invit work"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&piv, (size_t)n * T, stream), "malloc piv"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&Z, 8ULL * n * n * nk, stream), "malloc Z"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
     tri_prep_kernel<<<(int)((T + 255) / 256), 256, 0, stream>>>(d, e, n, nk, df, ef);
@@ -753,11 +753,11 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
     float2 *V = nullptr, *Gm = nullptr, *Tm = nullptr, *W1 = nullptr, *W2 = nullptr;
     const size_t nb = kWyBlock;
-    if ((st = cuda_check(cudaMallocAsync((void**)&V, 8ULL * nb * n * nk, stream), "malloc V"))) return st;
-    if ((st = cuda_check(cudaMallocAsync((void**)&Gm, 8ULL * nb * nb * nk, stream), "malloc G"))) return st;
-    if ((st = cuda_check(cudaMallocAsync((void**)&Tm, 8ULL * nb * nb * nk, stream), "malloc T"))) return st;
-    if ((st = cuda_check(cudaMallocAsync((void**)&W1, 8ULL * nb * n * nk, stream), "malloc W1"))) return st;
-    if ((st = cuda_check(cudaMallocAsync((void**)&W2, 8ULL * nb * n * nk, stream), "malloc W2"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&V, 8ULL * nb * n * nk, stream), "malloc V"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Gm, 8ULL * nb * nb * nk, stream), "malloc G"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Tm, 8ULL * nb * nb * nk, stream), "malloc T"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&W1, 8ULL * nb * n * nk, stream), "malloc W1"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&W2, 8ULL * nb * n * nk, stream), "malloc W2"))) return st;
     auto* Vc = reinterpret_cast<cuComplex*>(V);
     auto* Gc = reinterpret_cast<cuComplex*>(Gm);
     auto* Tc = reinterpret_cast<cuComplex*>(Tm);
