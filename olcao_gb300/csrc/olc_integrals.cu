@@ -14,6 +14,7 @@
 //   applyPhaseFactors, kPointLatticeOriginShift and saveCurrentPair
 //   (intgSaving.F90:95-505) -- out(m1,m2,k) = e^{ik.L} sum_R e^{ik.R} block_R
 //   written straight into valeVale / coreVale / coreCore.
+#include <type_traits>
 #include <cstdio>
 
 #include "olc_common.h"
@@ -115,20 +116,24 @@ struct PrimArgs {
   int ep_alpha;             // EP: exponent index of a single term
 };
 
-template <int OP, int L1, int L2>
+// MODE 0: every term in FP64.  Mixed precision splits the electronic
+// potential into two passes: MODE 1 the near images (FP64), MODE 2 the images
+// past the far-shell cut (FP32 accumulator), added to the same blocks.
+template <int OP, int L1, int L2, int MODE>
 __global__ void __launch_bounds__(128) prim_kernel(SysView v, PrimArgs a) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= a.n) return;
   constexpr int N1 = ncart(L1), N2 = ncart(L2), NS = nharm(L1) * nharm(L2);
   ItemGeom g;
   load_item(v, a.task[idx], a.ab[idx], g);
-  double cart[N1 * N2];
+  using R = typename std::conditional<MODE == 2, float, double>::type;
+  R cart[N1 * N2];
 #pragma unroll
-  for (int q = 0; q < N1 * N2; ++q) cart[q] = 0.0;
+  for (int q = 0; q < N1 * N2; ++q) cart[q] = R(0);
   double scale = 1.0;
-  if (OP == OLC_OP_OVERLAP) {
+  if constexpr (OP == OLC_OP_OVERLAP) {
     add_overlap<L1, L2>(g.a1, g.a2, g.A, g.B, 1.0, cart);
-  } else if (OP == OLC_OP_KINETIC) {
+  } else if constexpr (OP == OLC_OP_KINETIC) {
     add_kinetic<L1, L2>(g.a1, g.a2, g.A, g.B, 1.0, cart);
   } else {
     // centre of the alpha-pair overlap (alphaCenter, gaussRelations.f90:122)
@@ -139,7 +144,7 @@ __global__ void __launch_bounds__(128) prim_kernel(SysView v, PrimArgs a) {
     for (int c = 0; c < 3; ++c) P[c] = cen * (g.A[c] - g.B[c]) + g.B[c];
     const double frac = 1.0 - g.sep / alpha_dist(v, g.ia1, g.ia2, g.e1, g.e2);
     const double T = v.log_thresh;
-    if (OP == OLC_OP_NUCLEAR) {
+    if constexpr (OP == OLC_OP_NUCLEAR) {
       for (int m = 0; m < v.num_pot_sites; ++m) {
         const DevPotType& pt = v.pot_types[v.pot_site_type[m]];
         if (pt.nuc_charge < 1.0e-8) continue;
@@ -171,17 +176,28 @@ __global__ void __launch_bounds__(128) prim_kernel(SysView v, PrimArgs a) {
               const double tad = frac * (T * (al + ak + pe[j]) / (al + ak) / pe[j]);
               if (dd > tad) break;
               const double w = a.coeffs ? a.coeffs[pt.cumul_alpha + j] : 1.0;
-              add_elec3c<L1, L2, double>(g.a1, g.a2, pt.alphas[j], g.A, g.B, Cp, expAB, w, cart);
+              if constexpr (MODE == 0) {
+                add_elec3c<L1, L2, double>(g.a1, g.a2, pt.alphas[j], g.A, g.B, Cp, expAB, w, cart);
+              } else {
+                const double rho = elec3c_rho(g.a1, g.a2, pt.alphas[j], g.A, g.B, Cp);
+                if constexpr (MODE == 1) {
+                  if (rho <= kFarRho)
+                    add_elec3c<L1, L2, double>(g.a1, g.a2, pt.alphas[j], g.A, g.B, Cp, expAB, w, cart);
+                } else {
+                  if (rho > kFarRho)
+                    add_elec3c_f32<L1, L2>(g.a1, g.a2, pt.alphas[j], g.A, g.B, Cp, expAB, w, rho, cart);
+                }
+              }
             }
           });
         }
       }
     }
   }
-  store_harmonic<L1, L2, double>(cart, a.out + (size_t)idx * NS, a.accumulate != 0, scale);
+  store_harmonic<L1, L2, R>(cart, a.out + (size_t)idx * NS, a.accumulate != 0, scale);
 }
 
-template <int OP>
+template <int OP, int MODE>
 int launch_class(olc_context* ctx, int cls, const double* coeffs, int ep_type, int ep_alpha,
                  bool accumulate) {
   const ItemLists& it = ctx->items;
@@ -199,7 +215,7 @@ int launch_class(olc_context* ctx, int cls, const double* coeffs, int ep_type, i
   StageScope scope(ctx, OLC_STAGE_PRIMITIVES);
   switch (cls) {
 #define OLC_CASE(c, l1, l2) \
-  case c: prim_kernel<OP, l1, l2><<<grid, block, 0, ctx->stream>>>(ctx->view, a); break;
+  case c: prim_kernel<OP, l1, l2, MODE><<<grid, block, 0, ctx->stream>>>(ctx->view, a); break;
     OLC_CASE(0, 0, 0) OLC_CASE(1, 0, 1) OLC_CASE(2, 0, 2)
     OLC_CASE(3, 1, 0) OLC_CASE(4, 1, 1) OLC_CASE(5, 1, 2)
     OLC_CASE(6, 2, 0) OLC_CASE(7, 2, 1) OLC_CASE(8, 2, 2)
@@ -221,14 +237,22 @@ int run_primitives(olc_context* ctx, int op, int term, const double* coeffs, int
       }
     if (ep_type < 0) return fail(OLC_ERR_ARG, "potential term index out of range");
   }
-  (void)precision;
+  // OLC_PREC_MIXED: far-shell electronic-potential images in FP32
+  const bool far32 = precision == OLC_PREC_MIXED;
   for (int cls = 0; cls < kNumClasses; ++cls) {
     int st = 0;
     switch (op) {
-      case OLC_OP_OVERLAP: st = launch_class<OLC_OP_OVERLAP>(ctx, cls, nullptr, -1, 0, accumulate); break;
-      case OLC_OP_KINETIC: st = launch_class<OLC_OP_KINETIC>(ctx, cls, nullptr, -1, 0, accumulate); break;
-      case OLC_OP_NUCLEAR: st = launch_class<OLC_OP_NUCLEAR>(ctx, cls, nullptr, -1, 0, accumulate); break;
-      case OLC_OP_ELECPOT: st = launch_class<OLC_OP_ELECPOT>(ctx, cls, coeffs, ep_type, ep_alpha, accumulate); break;
+      case OLC_OP_OVERLAP: st = launch_class<OLC_OP_OVERLAP, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_KINETIC: st = launch_class<OLC_OP_KINETIC, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_NUCLEAR: st = launch_class<OLC_OP_NUCLEAR, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_ELECPOT:
+        if (far32) {
+          st = launch_class<OLC_OP_ELECPOT, 1>(ctx, cls, coeffs, ep_type, ep_alpha, accumulate);
+          if (!st) st = launch_class<OLC_OP_ELECPOT, 2>(ctx, cls, coeffs, ep_type, ep_alpha, true);
+        } else {
+          st = launch_class<OLC_OP_ELECPOT, 0>(ctx, cls, coeffs, ep_type, ep_alpha, accumulate);
+        }
+        break;
       default: return fail(OLC_ERR_ARG, "unknown integral operator");
     }
     if (st) return st;

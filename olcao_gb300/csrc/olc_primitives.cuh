@@ -211,6 +211,51 @@ __device__ __forceinline__ void add_elec3c(double a1, double a2, double a3, cons
       cart[a * N2 + b] += pref * s[0][cex(a)][cex(b)] * s[1][cey(a)][cey(b)] * s[2][cez(a)][cez(b)];
 }
 
+// Far-shell split of add_elec3c.  With rho = z a3 / z3 |P - C|^2 an image
+// enters with the suppression exp(-rho); images past kFarRho (exp(-22) =
+// 2.8e-10) may run in FP32 (GB300's FP32 rate is 64x its FP64 rate).  Their
+// FP32 rounding, 6e-8 of a term that the suppression and the recurrence's
+// polynomial in the image distance (up to 25^4 for d-d at the cut-off
+// radius) keep below ~3e-6 of the block scale, stays near 2e-13 of it.
+constexpr double kFarRho = 22.0;
+
+__device__ __forceinline__ double elec3c_rho(double a1, double a2, double a3, const double* A,
+                                             const double* B, const double* Cc) {
+  const double z = a1 + a2;
+  double pc2 = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double P = (a1 * A[c] + a2 * B[c]) / z;
+    pc2 += (P - Cc[c]) * (P - Cc[c]);
+  }
+  return z * a3 / (z + a3) * pc2;
+}
+
+// add_elec3c for a far image, in FP32 (rho from elec3c_rho).
+template <int L1, int L2>
+__device__ __forceinline__ void add_elec3c_f32(double a1, double a2, double a3, const double* A,
+                                               const double* B, const double* Cc, double expAB,
+                                               double w, double rho, float* cart) {
+  constexpr int N1 = ncart(L1), N2 = ncart(L2);
+  const float iz3 = 1.0f / (float)(a1 + a2 + a3);
+  float s[3][L1 + 1][L2 + 1];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    // G - A = (a2 (B - A) + a3 (C - A)) / z3, G - B = (-a1 (B - A) + a3 (C - B)) / z3
+    const float ba = (float)(B[c] - A[c]), ca = (float)(Cc[c] - A[c]), cb = (float)(Cc[c] - B[c]);
+    const float ga = ((float)a2 * ba + (float)a3 * ca) * iz3;
+    const float gb = (-(float)a1 * ba + (float)a3 * cb) * iz3;
+    os1d<L1, L2, float>(ga, gb, 0.5f * iz3, s[c]);
+  }
+  const float r = 3.14159265358979f * iz3;
+  const float pref = (float)(w * expAB) * r * sqrtf(r) * expf(-(float)rho);
+#pragma unroll
+  for (int a = 0; a < N1; ++a)
+#pragma unroll
+    for (int b = 0; b < N2; ++b)
+      cart[a * N2 + b] += pref * s[0][cex(a)][cex(b)] * s[1][cey(a)][cey(b)] * s[2][cez(a)][cez(b)];
+}
+
 // ---------------------------------------------------------------------------
 // Boys function F_0..F_n in the reference's formulation
 // ---------------------------------------------------------------------------

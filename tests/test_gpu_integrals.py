@@ -96,3 +96,18 @@ def test_hamiltonian_fused_equals_sum(pair):
     if o.core_dim:
         _cmp(hc, acc[1], "fused H coreVale")
         _cmp(hcc, acc[2], "fused H coreCore")
+
+
+@pytest.mark.gpu
+def test_elecpot_far_shell_fp32_matches_fp64(pair):
+    """Mixed precision evaluates images past the far-shell cut in FP32; the
+    blocks stay within the FP64 bar of the oracle."""
+    from olcao_gb300 import api
+    sysm, o, ctx = pair
+    for term in sorted({0, o.pot_dim - 1}):
+        vv, cv, cc = ctx.gauss_overlap(4, term, precision=api.PREC_MIXED)
+        rv, rc, rcc = o.operator(4, term)
+        _cmp(vv, rv, f"EP{term} mixed valeVale")
+        if o.core_dim:
+            _cmp(cv, rc, f"EP{term} mixed coreVale")
+            _cmp(cc, rcc, f"EP{term} mixed coreCore")

@@ -124,3 +124,15 @@ def test_zero_coefficient_rule(case):
     assert np.abs(ctx.scf_iteration(c, o.vale_dim) - w0).max() <= EIG_TOL
     ctx.scf_prepare(api.PREC_FP64, api.FORM_FUSED)
     assert np.abs(ctx.scf_iteration(c, o.vale_dim) - _fused_reference(o, c)).max() <= EIG_TOL
+
+
+@pytest.mark.gpu
+def test_scf_iteration_fused_mixed(case):
+    """Fused form with mixed precision (far-shell potential images in FP32,
+    mixed solver where n > 64): eigenvalues within the mixed bar of the
+    fused FP64 semantics."""
+    from olcao_gb300 import api
+    sysm, o, packed, hp, w, ctx = case
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_FUSED)
+    eig = ctx.scf_iteration(sysm.pot_coeffs, o.vale_dim, precision=api.PREC_MIXED)
+    assert np.abs(eig - _fused_reference(o, sysm.pot_coeffs)).max() <= 1e-6
