@@ -188,6 +188,11 @@ typedef enum {
 /* Flags of olc_scf_iteration. */
 #define OLC_ITER_EIG_DEVICE   1   /* eigenvalues pointer is device memory    */
 #define OLC_ITER_COEFF_DEVICE 2   /* coeffs pointer is device memory         */
+#define OLC_ITER_GRAPH        4   /* mixed stored-form pass as a CUDA graph:
+                                     the first call for a num_states / vectors
+                                     choice runs directly, the second captures,
+                                     later calls replay (direct launches if the
+                                     capture is refused)                      */
 
 /* Set-up of the iteration-invariant parts of the SCF pass: S(k) orthogonalised,
  * H0 = ortho(KE + NP), and for OLC_FORM_STORED every orthogonalised, packed

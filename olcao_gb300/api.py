@@ -37,7 +37,7 @@ LIB_PATH = os.path.join(HERE, "libolcao_gb300.so")
 OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT, OP_HAMILTONIAN = 1, 2, 3, 4, 6
 PREC_FP64, PREC_MIXED = 0, 1
 FORM_FUSED, FORM_STORED = 0, 1
-ITER_EIG_DEVICE, ITER_COEFF_DEVICE = 1, 2
+ITER_EIG_DEVICE, ITER_COEFF_DEVICE, ITER_GRAPH = 1, 2, 4
 
 EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_get_dims", "olc_set_stream", "olc_gauss_overlap",
@@ -316,10 +316,12 @@ class Context:
         return H.T.copy(), Sm.T.copy()
 
     def scf_iteration(self, coeffs, num_states: int, precision: int = PREC_FP64,
-                      eig_out=None, vectors=None):
+                      eig_out=None, vectors=None, graph: bool = False):
         """One SCF pass; returns eigenvalues [nk, num_states].  coeffs and
-        eig_out may each be host numpy arrays or device tensors."""
-        flags = 0
+        eig_out may each be host numpy arrays or device tensors.  graph=True
+        runs the mixed stored-form pass as a CUDA graph (captured on the
+        second call for a given num_states / vectors choice)."""
+        flags = ITER_GRAPH if graph else 0
         if isinstance(coeffs, np.ndarray) or not hasattr(coeffs, "data_ptr"):
             co = np.ascontiguousarray(coeffs, np.float64)
             cptr = co.ctypes.data

@@ -46,7 +46,7 @@ void count_launch(int n) { g_launches += n; }
 StageScope::StageScope(olc_context* ctx, int stage, int launches)
     : ctx_(ctx), stage_(stage), launches_(launches) {
   count_launch(launches);
-  if (ctx_ && ctx_->profiling) {
+  if (ctx_ && ctx_->profiling && !ctx_->capturing) {
     a_ = take_event(ctx_);
     cudaEventRecord(a_, ctx_->stream);
   }
@@ -182,6 +182,7 @@ int olc_destroy(olc_context_t* ctx) {
     cudaEventDestroy(ctx->mixed_join[i]);
   }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   if (ctx->blas) cublasDestroy(ctx->blas);
   if (ctx->blas_f32) cublasDestroy(ctx->blas_f32);
   if (ctx->pool) {

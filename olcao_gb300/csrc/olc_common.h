@@ -112,6 +112,14 @@ struct olc_context {
   cublasHandle_t blas = nullptr;
   cublasHandle_t blas_f32 = nullptr;   // FP32 products (BF16x9 emulation)
   cudaMemPool_t pool = nullptr;        // scratch of the SCF pass, kept between calls
+  // CUDA graph of the mixed stored-form pass (OLC_ITER_GRAPH)
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_key = -1, graph_warm = -1;
+  bool graph_broken = false, capturing = false;
+  int64_t graph_launches = 0;
+  double* g_coeff = nullptr;
+  double* g_eig = nullptr;
+  double* g_vec = nullptr;
   cusolverDnHandle_t solver = nullptr;
   // host copies
   olc_dims_t dims{};
@@ -262,6 +270,9 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
                 int nb, int stage = OLC_STAGE_REFINE);
 void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
+
+// status of a queued mixed solve (olc_mixed.cu)
+int mixed_check_info(olc_context* ctx);
 
 // raw layout-identical dataset writer (olc_layout.cu)
 int write_setup_integrals(olc_context* ctx, const char* root);

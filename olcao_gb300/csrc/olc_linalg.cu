@@ -342,7 +342,7 @@ int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
 }
 
 int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
-                     double* eig_dev, double* vectors);
+                     double* eig_dev, double* vectors, bool check = true);
 
 int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* eigenvalues,
                int eig_on_device, double* vectors, int32_t* info, int precision = OLC_PREC_FP64) {
@@ -524,11 +524,95 @@ int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, 
   return st ? st : s2;
 }
 
+// The mixed, stored-form pass queued on the context stream without any host
+// synchronisation (the part a CUDA graph captures): H(k) from the resident
+// terms with the device coefficients, then the mixed solve.
+static int enqueue_mixed_pass(olc_context* ctx, const double* dcoeffs, int num_states, double* eig_dev,
+                              double* vectors) {
+  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
+  const size_t nn = (size_t)nv * nv;
+  int st;
+  double *h = nullptr, *s = nullptr;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
+  if ((st = build_hamiltonian(ctx, dcoeffs, OLC_PREC_MIXED, OLC_ITER_COEFF_DEVICE, h))) return st;
+  cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
+  st = solve_full_mixed(ctx, h, s, num_states, eig_dev, vectors, false);
+  cudaFreeAsync(h, ctx->stream);
+  cudaFreeAsync(s, ctx->stream);
+  return st;
+}
+
+// OLC_ITER_GRAPH: the mixed stored-form pass as a CUDA graph.  Inputs and
+// outputs go through fixed context buffers; the first call for a given
+// (num_states, vectors) runs the pass directly (library workspaces get
+// allocated), the second captures it, later calls replay it.  If the capture
+// is refused, the context keeps running the pass directly.
+static int scf_iteration_graph(olc_context* ctx, const double* coeffs, int num_states,
+                               double* eigenvalues, int flags, double* vectors) {
+  const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints, pd = ctx->dims.pot_dim;
+  cudaStream_t stream = ctx->stream;
+  int st;
+  if (!ctx->g_coeff && (st = dalloc(ctx, &ctx->g_coeff, (size_t)std::max(1, pd)))) return st;
+  if (!ctx->g_eig && (st = dalloc(ctx, &ctx->g_eig, (size_t)nv * nk))) return st;
+  if (vectors && !ctx->g_vec && (st = dalloc(ctx, &ctx->g_vec, 2 * (size_t)nv * nv * nk))) return st;
+  cudaMemcpyAsync(ctx->g_coeff, coeffs, sizeof(double) * pd,
+                  (flags & OLC_ITER_COEFF_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream);
+  double* vout = vectors ? ctx->g_vec : nullptr;
+  const int key = num_states * 2 + (vectors ? 1 : 0);
+  if (ctx->graph_exec && ctx->graph_key != key) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  if (!ctx->graph_exec) {
+    if (ctx->graph_warm != key || ctx->graph_broken) {
+      // direct pass (first call for this key, or capture refused before)
+      if ((st = enqueue_mixed_pass(ctx, ctx->g_coeff, num_states, ctx->g_eig, vout))) return st;
+      ctx->graph_warm = key;
+    } else {
+      const int64_t l0 = olc_launch_count();
+      ctx->capturing = true;
+      cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+      int sq = e == cudaSuccess ? enqueue_mixed_pass(ctx, ctx->g_coeff, num_states, ctx->g_eig, vout) : 1;
+      cudaGraph_t g = nullptr;
+      if (e == cudaSuccess) e = cudaStreamEndCapture(stream, &g);
+      ctx->capturing = false;
+      const int64_t captured = olc_launch_count() - l0;
+      count_launch(-(int)captured);      // nothing ran yet
+      if (!sq && e == cudaSuccess && g) e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (sq || e != cudaSuccess || !ctx->graph_exec) {
+        cudaGetLastError();
+        ctx->graph_exec = nullptr;
+        ctx->graph_broken = true;
+        if ((st = enqueue_mixed_pass(ctx, ctx->g_coeff, num_states, ctx->g_eig, vout))) return st;
+      } else {
+        ctx->graph_key = key;
+        ctx->graph_launches = captured;
+      }
+    }
+  }
+  if (ctx->graph_exec) {
+    if ((st = cuda_check(cudaGraphLaunch(ctx->graph_exec, stream), "graph launch"))) return st;
+    count_launch((int)ctx->graph_launches);
+  }
+  if ((st = mixed_check_info(ctx))) return st;
+  const size_t ebytes = sizeof(double) * (size_t)num_states * nk;
+  cudaMemcpyAsync(eigenvalues, ctx->g_eig, ebytes,
+                  (flags & OLC_ITER_EIG_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream);
+  if (vectors)
+    cudaMemcpyAsync(vectors, ctx->g_vec, 16 * (size_t)nv * num_states * nk, cudaMemcpyDeviceToDevice, stream);
+  return cuda_check(cudaStreamSynchronize(stream), "graph pass sync");
+}
+
 int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
                   double* eigenvalues, int flags, double* vectors) {
   if (!ctx->prepared) return fail(OLC_ERR_ARG, "olc_scf_iteration before olc_scf_prepare");
   const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   if (num_states < 1 || num_states > nv) return fail(OLC_ERR_ARG, "num_states out of range");
+  if ((flags & OLC_ITER_GRAPH) && precision == OLC_PREC_MIXED && ctx->prep_form == OLC_FORM_STORED &&
+      nv > small_solver_max_n())
+    return scf_iteration_graph(ctx, coeffs, num_states, eigenvalues, flags, vectors);
   const size_t nn = (size_t)nv * nv;
   int st;
   double *h = nullptr, *s = nullptr;

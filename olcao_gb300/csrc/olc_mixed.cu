@@ -721,7 +721,7 @@ static bool use_batched_fp32(int n) {
 // Solve every k with the mixed-precision scheme; h, s are full Hermitian
 // FP64 [nk][n][n] (not modified).
 int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
-                     double* eig_dev, double* vectors) {
+                     double* eig_dev, double* vectors, bool check) {
   const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   if (n > kSortMax) return fail(OLC_ERR_UNSUPPORTED, "mixed solver: n above 8192");
   const size_t nn = (size_t)n * n;
@@ -826,11 +826,18 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   cudaFreeAsync(Hh, stream);
   cudaFreeAsync(Sh, stream);
   cudaFreeAsync(X, stream);
+  if (st || !check) return st;
+  return mixed_check_info(ctx);
+}
+
+// Waits for the queued mixed solve and turns the FP32 factorisation's info
+// codes into a status.
+int mixed_check_info(olc_context* ctx) {
+  const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   std::vector<int> hinfo(nk);
-  cudaMemcpyAsync(hinfo.data(), ctx->d_info, sizeof(int) * nk, cudaMemcpyDeviceToHost, stream);
-  int s2 = cuda_check(cudaStreamSynchronize(stream), "mixed solve sync");
+  cudaMemcpyAsync(hinfo.data(), ctx->d_info, sizeof(int) * nk, cudaMemcpyDeviceToHost, ctx->stream);
+  int st = cuda_check(cudaStreamSynchronize(ctx->stream), "mixed solve sync");
   if (st) return st;
-  if (s2) return s2;
   for (int k = 0; k < nk; ++k) {
     if (hinfo[k] > n) return fail(OLC_ERR_NOT_PD, "overlap matrix not positive definite (FP32 factorisation)");
     if (hinfo[k] != 0) return fail(OLC_ERR_EIGEN, "FP32 eigen-solver did not converge");

@@ -68,3 +68,31 @@ def test_mixed_solver_matches_fp64_path(gpu_lib, name):
         assert np.abs(G - np.eye(n)).max() < 1e-4
         R = H @ Z - Sm @ Z * wm[k][None, :]
         assert np.abs(R).max() < 1e-3
+
+
+@pytest.mark.gpu
+def test_graph_replay_matches_direct_pass(gpu_lib):
+    """OLC_ITER_GRAPH: direct first call, capture on the second, replays
+    after; every call gives the direct pass's eigenvalues for its inputs
+    (within the mixed path's run-to-run spread: the FP32 reduction sums with
+    shared-memory atomics) and launches the same number of kernels of this
+    library."""
+    import torch
+    from olcao_gb300 import api
+    sysm = S.CONFIGS["si8"]()
+    sysm.kpoints_abc = sysm.kpoints_abc[:16]
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n = ctx.vale_dim
+    vec = torch.zeros(ctx.nk, n, n, dtype=torch.complex128, device="cuda")
+    coeffs = [sysm.pot_coeffs * f for f in (1.0, 0.97, 1.02, 1.0)]
+    direct = [ctx.scf_iteration(c, n, precision=api.PREC_MIXED, vectors=vec) for c in coeffs]
+    l0 = api.launch_count()
+    ctx.scf_iteration(coeffs[0], n, precision=api.PREC_MIXED, vectors=vec)
+    per_pass = api.launch_count() - l0
+    for i, c in enumerate(coeffs):
+        l0 = api.launch_count()
+        w = ctx.scf_iteration(c, n, precision=api.PREC_MIXED, vectors=vec, graph=True)
+        assert np.abs(w - direct[i]).max() <= 1e-7
+        if i >= 1:                     # captured and replayed
+            assert api.launch_count() - l0 == per_pass
