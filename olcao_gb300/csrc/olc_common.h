@@ -120,6 +120,8 @@ struct olc_context {
   double* g_coeff = nullptr;
   double* g_eig = nullptr;
   double* g_vec = nullptr;
+  // tuned CTAs per k of the FP32 tridiagonalisation (olc_tridiag.cu)
+  int trd_tuned_n = 0, trd_tuned_nk = 0, trd_tuned_g = 0;
   cusolverDnHandle_t solver = nullptr;
   // host copies
   olc_dims_t dims{};

@@ -639,6 +639,71 @@ int hetrd_max_n() {
   return (smem - 2048) / (4 * (int)sizeof(float2));
 }
 
+// One tridiagonalisation launch with clusters of G CTAs (one cluster per k).
+static int launch_hetrd(olc_context* ctx, int G, float2* H, int n, int ld, int nk, size_t smem, double* d,
+                        double* e, float2* tau) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(G, nk, 1);
+  cfg.blockDim = dim3(kTrdThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel, H, n, ld, d, e, tau), "hetrd launch");
+}
+
+// Autotuner of the CTAs per k: the first pass of a context for a given
+// (n, nk) times every candidate cluster size that keeps the launch within two
+// waves, each on a copy of the reduced matrices, and keeps the fastest.
+static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk, size_t smem, double* d,
+                        double* e, float2* tau, int* G) {
+  if (ctx->trd_tuned_n == n && ctx->trd_tuned_nk == nk) {
+    *G = ctx->trd_tuned_g;
+    return OLC_OK;
+  }
+  int cand[4], nc = 0;
+  for (int g = 1; g <= 8; g *= 2)
+    if (g * nk <= 2 * 152 && (g * nk >= 38 || g == 8)) cand[nc++] = g;
+  if (!nc) cand[nc++] = 1;
+  int best = cand[0];
+  if (nc > 1) {
+    const size_t bytes = sizeof(float2) * (size_t)n * ld * nk;
+    float2* scratch = nullptr;
+    int st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&scratch, bytes, ctx->stream), "malloc tuning copy"))) return st;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best_ms = 1e30f;
+    for (int i = 0; i < nc; ++i) {
+      cudaMemcpyAsync(scratch, H, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+      cudaEventRecord(a, ctx->stream);
+      st = launch_hetrd(ctx, cand[i], scratch, n, ld, nk, smem, d, e, tau);
+      cudaEventRecord(b, ctx->stream);
+      if (!st) st = cuda_check(cudaEventSynchronize(b), "tuning sync");
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      count_launch();
+      if (st) break;
+      if (ms < best_ms) { best_ms = ms; best = cand[i]; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFreeAsync(scratch, ctx->stream);
+    if (st) return st;
+  }
+  ctx->trd_tuned_n = n;
+  ctx->trd_tuned_nk = nk;
+  ctx->trd_tuned_g = best;
+  *G = best;
+  return OLC_OK;
+}
+
 // FP32 eigenvectors X (S-orthonormal, [nk][n][n] complex column-major) of
 // every pencil (h32, s32).  h32 and s32 are overwritten (reduced matrix and
 // reflectors; Cholesky factor).  ctx->d_info receives potrf's info per k.
@@ -699,30 +764,16 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
   {
     StageScope scope(ctx, OLC_STAGE_SOLVE, 1);
-    // CTAs per k: enough clusters to fill the SMs (OLC_TRD_CLUSTER overrides)
-    int G = 1;
-    while (G < 8 && (G * 2) * nk <= 152) G *= 2;
+    const size_t smem = 4 * sizeof(float2) * (size_t)ld;
+    if ((st = cuda_check(cudaFuncSetAttribute(hetrd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem), "hetrd smem"))) return st;
+    int G = 0;
     if (const char* v = std::getenv("OLC_TRD_CLUSTER")) {
       const int g = std::atoi(v);
       if (g == 1 || g == 2 || g == 4 || g == 8) G = g;
     }
-    const size_t smem = 4 * sizeof(float2) * (size_t)ld;
-    auto kern = hetrd_kernel;
-    if ((st = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                         "hetrd smem"))) return st;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(G, nk, 1);
-    cfg.blockDim = dim3(kTrdThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = G;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if ((st = cuda_check(cudaLaunchKernelEx(&cfg, kern, H, n, ld, d, e, tau), "hetrd launch"))) return st;
+    if (!G && (st = tune_cluster(ctx, H, n, ld, nk, smem, d, e, tau, &G))) return st;
+    if ((st = launch_hetrd(ctx, G, H, n, ld, nk, smem, d, e, tau))) return st;
   }
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
   const size_t T = (size_t)n * nk;
