@@ -120,6 +120,10 @@ struct olc_context {
   double* g_coeff = nullptr;
   double* g_eig = nullptr;
   double* g_vec = nullptr;
+  // FP32 Cholesky factors of the prepared S(k) (they do not change between
+  // SCF passes): [nk][n][ld], valid after the first mixed pass
+  float* u32 = nullptr;
+  bool u32_valid = false;
   // tuned CTAs per k of the FP32 tridiagonalisation (olc_tridiag.cu)
   int trd_tuned_n = 0, trd_tuned_nk = 0, trd_tuned_g = 0;
   cusolverDnHandle_t solver = nullptr;
@@ -283,6 +287,7 @@ int write_eigen(const char* root, int nk, int spin, int num_states, int vale_dim
 
 // batched FP32 eigen-solve (olc_tridiag.cu)
 int hetrd_max_n();
-int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X);
+int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X,
+                       const float* u_cached, float* u_store);
 
 }  // namespace olc

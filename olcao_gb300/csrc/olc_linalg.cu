@@ -342,10 +342,11 @@ int solve_full_library(olc_context* ctx, double* h, double* s, int num_states,
 }
 
 int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
-                     double* eig_dev, double* vectors, bool check = true);
+                     double* eig_dev, double* vectors, bool check = true, bool s_prepared = false);
 
 int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* eigenvalues,
-               int eig_on_device, double* vectors, int32_t* info, int precision = OLC_PREC_FP64) {
+               int eig_on_device, double* vectors, int32_t* info, int precision = OLC_PREC_FP64,
+               bool s_prepared = false) {
   const int n = ctx->dims.vale_dim;
   if (precision == OLC_PREC_MIXED && n > small_solver_max_n()) {
     int st;
@@ -357,7 +358,7 @@ int solve_full(olc_context* ctx, double* h, double* s, int num_states, double* e
                                            ctx->stream), "malloc eigs"))) return st;
       eig_dev = tmp;
     }
-    st = solve_full_mixed(ctx, h, s, num_states, eig_dev, vectors);
+    st = solve_full_mixed(ctx, h, s, num_states, eig_dev, vectors, true, s_prepared);
     if (!eig_on_device) {
       cudaMemcpyAsync(eigenvalues, tmp, sizeof(double) * (size_t)num_states * nk,
                       cudaMemcpyDeviceToHost, ctx->stream);
@@ -498,6 +499,7 @@ int scf_prepare(olc_context* ctx, int precision, int form) {
                             nullptr, ctx->d_h0, nullptr))) return st;
   }
   ctx->prepared = true;
+  ctx->u32_valid = false;
   ctx->prep_precision = precision;
   ctx->prep_form = form;
   return cuda_check(cudaStreamSynchronize(ctx->stream), "prepare sync");
@@ -532,14 +534,12 @@ static int enqueue_mixed_pass(olc_context* ctx, const double* dcoeffs, int num_s
   const int nv = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   const size_t nn = (size_t)nv * nv;
   int st;
-  double *h = nullptr, *s = nullptr;
+  double* h = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
   if ((st = build_hamiltonian(ctx, dcoeffs, OLC_PREC_MIXED, OLC_ITER_COEFF_DEVICE, h))) return st;
-  cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
-  st = solve_full_mixed(ctx, h, s, num_states, eig_dev, vectors, false);
+  // the mixed solve reads S without modifying it: the prepared S directly
+  st = solve_full_mixed(ctx, h, ctx->d_chol, num_states, eig_dev, vectors, false, true);
   cudaFreeAsync(h, ctx->stream);
-  cudaFreeAsync(s, ctx->stream);
   return st;
 }
 
@@ -615,15 +615,18 @@ int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num
     return scf_iteration_graph(ctx, coeffs, num_states, eigenvalues, flags, vectors);
   const size_t nn = (size_t)nv * nv;
   int st;
+  // the FP64 solvers overwrite S with its factor and need a copy; the mixed
+  // solver (n above the small solver's limit) reads the prepared S directly
+  const bool mixed = precision == OLC_PREC_MIXED && nv > small_solver_max_n();
   double *h = nullptr, *s = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&h, 16 * nn * nk, ctx->stream), "malloc h"))) return st;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
+  if (!mixed && (st = cuda_check(ctx_malloc(ctx, (void**)&s, 16 * nn * nk, ctx->stream), "malloc s"))) return st;
   if ((st = build_hamiltonian(ctx, coeffs, precision, flags, h))) return st;
-  cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
-  st = solve_full(ctx, h, s, num_states, eigenvalues, (flags & OLC_ITER_EIG_DEVICE) ? 1 : 0,
-                  vectors, nullptr, precision);
+  if (!mixed) cudaMemcpyAsync(s, ctx->d_chol, 16 * nn * nk, cudaMemcpyDeviceToDevice, ctx->stream);
+  st = solve_full(ctx, h, mixed ? ctx->d_chol : s, num_states, eigenvalues,
+                  (flags & OLC_ITER_EIG_DEVICE) ? 1 : 0, vectors, nullptr, precision, mixed);
   cudaFreeAsync(h, ctx->stream);
-  cudaFreeAsync(s, ctx->stream);
+  if (s) cudaFreeAsync(s, ctx->stream);
   int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "iteration sync");
   return st ? st : s2;
 }

@@ -721,31 +721,42 @@ static bool use_batched_fp32(int n) {
 // Solve every k with the mixed-precision scheme; h, s are full Hermitian
 // FP64 [nk][n][n] (not modified).
 int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num_states,
-                     double* eig_dev, double* vectors, bool check) {
+                     double* eig_dev, double* vectors, bool check, bool s_prepared) {
   const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   if (n > kSortMax) return fail(OLC_ERR_UNSUPPORTED, "mixed solver: n above 8192");
   const size_t nn = (size_t)n * n;
   int st;
   cudaStream_t stream = ctx->stream;
   // ---- 1. FP32 generalised solve per k -----------------------------------
+  // the prepared S(k) does not change between passes: its FP32 Cholesky
+  // factors are kept from the first pass
+  const bool batched = use_batched_fp32(n);
+  const bool cached = batched && s_prepared && ctx->u32_valid;
   float *h32 = nullptr, *s32 = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
+  if (!cached && (st = cuda_check(ctx_malloc(ctx, (void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 2);
+    StageScope scope(ctx, OLC_STAGE_SOLVE, cached ? 1 : 2);
     to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
-    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
+    if (!cached) to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
   }
   float* X = nullptr;      // FP32 eigenvectors, [nk][n][n] complex
-  if (use_batched_fp32(n)) {
+  if (batched) {
+    float* store = nullptr;
+    if (s_prepared && !cached) {
+      const size_t ld = (size_t)n + (n & 1);
+      if (!ctx->u32 && (st = dalloc(ctx, &ctx->u32, 2 * (size_t)n * ld * nk))) return st;
+      store = ctx->u32;
+    }
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
-    if ((st = solve_fp32_batched(ctx, n, nk, h32, s32, X))) return st;
+    if ((st = solve_fp32_batched(ctx, n, nk, h32, s32, X, cached ? ctx->u32 : nullptr, store))) return st;
+    if (store) ctx->u32_valid = true;
     cudaFreeAsync(h32, stream);
   } else {
     if ((st = solve_fp32_library(ctx, n, nk, h32, s32))) return st;
     X = h32;
   }
-  cudaFreeAsync(s32, stream);
+  if (s32) cudaFreeAsync(s32, stream);
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
   double *Y = nullptr, *Hh = nullptr, *Sh = nullptr;
   // bits kept of FP64 and FP32 operands (OLC_SPLIT_BITS overrides the FP64 count)
@@ -839,6 +850,7 @@ int mixed_check_info(olc_context* ctx) {
   int st = cuda_check(cudaStreamSynchronize(ctx->stream), "mixed solve sync");
   if (st) return st;
   for (int k = 0; k < nk; ++k) {
+    if (hinfo[k] != 0) ctx->u32_valid = false;
     if (hinfo[k] > n) return fail(OLC_ERR_NOT_PD, "overlap matrix not positive definite (FP32 factorisation)");
     if (hinfo[k] != 0) return fail(OLC_ERR_EIGEN, "FP32 eigen-solver did not converge");
   }

@@ -707,7 +707,10 @@ static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk
 // FP32 eigenvectors X (S-orthonormal, [nk][n][n] complex column-major) of
 // every pencil (h32, s32).  h32 and s32 are overwritten (reduced matrix and
 // reflectors; Cholesky factor).  ctx->d_info receives potrf's info per k.
-int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X) {
+// s32 may be null when u_cached holds the factors (layout [nk][n][ld],
+// ld = n rounded up to even); u_store, when given, receives the factors.
+int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X,
+                       const float* u_cached, float* u_store) {
   cudaStream_t stream = ctx->stream;
   int st;
   if (n < 2) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver needs n >= 2");
@@ -718,20 +721,24 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   const size_t nn = (size_t)n * ld;
   float2 *H = reinterpret_cast<float2*>(h32), *Sm = reinterpret_cast<float2*>(s32);
   float2* Xc = reinterpret_cast<float2*>(X);
+  float2* Sq_alloc = nullptr;
   if (ld != n) {
     float2 *Hq = nullptr, *Sq = nullptr, *Xq = nullptr;
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&Hq, 8 * nn * nk, stream), "malloc padded H"))) return st;
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&Sq, 8 * nn * nk, stream), "malloc padded S"))) return st;
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&Xq, 8 * nn * nk, stream), "malloc padded X"))) return st;
     relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, n, ld, nk, Hq);
-    relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(Sm, n, n, ld, nk, Sq);
+    if (!u_cached)
+      relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(Sm, n, n, ld, nk, Sq);
     count_launch(2);
     H = Hq;
     Sm = Sq;
+    Sq_alloc = Sq;
     Xc = Xq;
   }
   float2** ptrs = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&ptrs, sizeof(float2*) * 3 * nk, stream), "malloc ptrs"))) return st;
+  if (u_cached) Sm = const_cast<float2*>(reinterpret_cast<const float2*>(u_cached));
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Sm, nn, nk, ptrs);
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(H, nn, nk, ptrs + nk);
   ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Xc, nn, nk, ptrs + 2 * nk);
@@ -745,9 +752,15 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
     cusolverDnSetStream(ctx->solver, stream);
     if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
-    if (cusolverDnCpotrfBatched(ctx->solver, CUBLAS_FILL_MODE_UPPER, n, Sp, ld, ctx->d_info, nk) !=
-        CUSOLVER_STATUS_SUCCESS)
-      return fail(OLC_ERR_CUDA, "cusolverDnCpotrfBatched failed");
+    if (!u_cached) {
+      if (cusolverDnCpotrfBatched(ctx->solver, CUBLAS_FILL_MODE_UPPER, n, Sp, ld, ctx->d_info, nk) !=
+          CUSOLVER_STATUS_SUCCESS)
+        return fail(OLC_ERR_CUDA, "cusolverDnCpotrfBatched failed");
+      if (u_store)
+        cudaMemcpyAsync(u_store, Sm, sizeof(float2) * nn * nk, cudaMemcpyDeviceToDevice, stream);
+    } else {
+      cudaMemsetAsync(ctx->d_info, 0, sizeof(int) * nk, stream);
+    }
     if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C,
                            CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Hp, ld, nk) != CUBLAS_STATUS_SUCCESS)
       return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-H H) failed");
@@ -856,7 +869,7 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
         Xc, n, ld, n, nk, reinterpret_cast<float2*>(X));
     count_launch();
     cudaFreeAsync(H, stream);
-    cudaFreeAsync(Sm, stream);
+    cudaFreeAsync(Sq_alloc, stream);
     cudaFreeAsync(Xc, stream);
   }
   cudaFreeAsync(d, stream);
