@@ -30,13 +30,10 @@
 #include <cuda_bf16.h>
 
 #include "olc_common.h"
-#include "olc_jacobi.cuh"
 
 namespace olc {
 
 namespace {
-
-using jac::cd;
 
 constexpr double kClusterGap = 5e-3;
 constexpr int kSortMax = 8192;      // n limit of the in-shared-memory sort

@@ -479,23 +479,57 @@ __global__ void invit_kernel(const double* __restrict__ d, const double* __restr
     s ^= s << 13; s ^= s >> 17; s ^= s << 5;
     x[(size_t)i * T + t] = (double)(s & 0xffffff) / 16777216.0 - 0.5;
   }
+  // the sweeps load their coefficients kInvChunk rows ahead of the
+  // dependent arithmetic (one memory latency per chunk instead of per row)
+  constexpr int kInvChunk = 8;
   for (int it = 0; it < 3; ++it) {
-    // forward: apply P and L
-    for (int i = 0; i < n - 1; ++i) {
-      const size_t o = (size_t)i * T + t, o1 = o + T;
-      double yi = x[o], yn = x[o1];
-      if (piv[o]) { const double tmp = yi; yi = yn; yn = tmp; x[o] = yi; }
-      x[o1] = yn - Lm[o] * yi;
+    // forward: apply P and L; yi carries the current row
+    double yi = x[t];
+    for (int i0 = 0; i0 < n - 1; i0 += kInvChunk) {
+      const int c = min(kInvChunk, n - 1 - i0);
+      double Lc[kInvChunk], yn[kInvChunk];
+      unsigned char pv[kInvChunk];
+#pragma unroll
+      for (int u = 0; u < kInvChunk; ++u)
+        if (u < c) {
+          const size_t o = (size_t)(i0 + u) * T + t;
+          Lc[u] = Lm[o];
+          pv[u] = piv[o];
+          yn[u] = x[o + T];
+        }
+#pragma unroll
+      for (int u = 0; u < kInvChunk; ++u)
+        if (u < c) {
+          double top = yi, bot = yn[u];
+          if (pv[u]) { top = yn[u]; bot = yi; }
+          x[(size_t)(i0 + u) * T + t] = top;
+          yi = bot - Lc[u] * top;
+        }
     }
+    x[(size_t)(n - 1) * T + t] = yi;
     // back substitution with U, scaled to max |x| = 1
     double x1 = 0.0, x2 = 0.0, amax = 0.0;
-    for (int i = n - 1; i >= 0; --i) {
-      const size_t o = (size_t)i * T + t;
-      const double xi = (x[o] - U1[o] * x1 - U2[o] * x2) * U0[o];
-      x[o] = xi;
-      x2 = x1;
-      x1 = xi;
-      amax = fmax(amax, fabs(xi));
+    for (int i0 = n - 1; i0 >= 0; i0 -= kInvChunk) {
+      const int c = min(kInvChunk, i0 + 1);
+      double xv[kInvChunk], u0[kInvChunk], u1[kInvChunk], u2[kInvChunk];
+#pragma unroll
+      for (int u = 0; u < kInvChunk; ++u)
+        if (u < c) {
+          const size_t o = (size_t)(i0 - u) * T + t;
+          xv[u] = x[o];
+          u0[u] = U0[o];
+          u1[u] = U1[o];
+          u2[u] = U2[o];
+        }
+#pragma unroll
+      for (int u = 0; u < kInvChunk; ++u)
+        if (u < c) {
+          const double xi = (xv[u] - u1[u] * x1 - u2[u] * x2) * u0[u];
+          x[(size_t)(i0 - u) * T + t] = xi;
+          x2 = x1;
+          x1 = xi;
+          amax = fmax(amax, fabs(xi));
+        }
     }
     const double sc = amax > 0.0 ? 1.0 / amax : 1.0;
     for (int i = 0; i < n; ++i) x[(size_t)i * T + t] *= sc;
