@@ -777,7 +777,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   if ((st = loewdin(ctx, n, nk, Hh, Sh, X))) return st;
   // ---- 4. clusters and their exact solves -----------------------------------
   ClusterLists L{};
-  L.cap = (n / 2 + 1) * nk;
+  L.cap = n * nk;                 // every cluster holds at least one state
   double *w_slot = nullptr, *v_slot = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.order, 4ULL * n * nk, stream), "malloc order"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.pos, 4ULL * n * nk, stream), "malloc pos"))) return st;
