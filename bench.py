@@ -147,7 +147,7 @@ def run_reference(args, world, rank):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     from olcao_gb300 import system as S
-    full = S.CONFIGS[args.config]()
+    full = S.SYSTEMS[args.config]()
     nk = full.num_kpoints
     ns = max(1, min(args.cpu_sample_k, nk))
     idx = np.linspace(0, nk - 1, ns).round().astype(int)
@@ -193,7 +193,7 @@ def run_ours(args, world, rank, dist):
         build.build()
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    full = S.CONFIGS[args.config]()
+    full = S.SYSTEMS[args.config]()
     if args.nk > 0:
         full.kpoints_abc = full.kpoints_abc[:args.nk]
     nk_total = full.num_kpoints

@@ -189,7 +189,7 @@ namespace olc {
 
 // Stream-ordered scratch from the context's own pool: the pool keeps freed
 // memory (release threshold = max), so repeated SCF passes do not go back to
-// the driver for their tens of GB of scratch.
+// the CUDA driver for their tens of GB of scratch.
 inline cudaError_t ctx_malloc(olc_context* ctx, void** p, size_t bytes, cudaStream_t s) {
   return ctx->pool ? cudaMallocFromPoolAsync(p, bytes, ctx->pool, s) : cudaMallocAsync(p, bytes, s);
 }

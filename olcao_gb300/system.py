@@ -341,7 +341,7 @@ def quartz(seed: int = 4, reps=3, sigma=0.05) -> System:
                    pot_of_type={0: 0, 1: 1})
 
 
-CONFIGS = {
+SYSTEMS = {
     "diamond": lambda: diamond(),
     "si64": lambda: silicon_supercell(2, 0.03, seed=2),
     "graphite": lambda: graphite(),

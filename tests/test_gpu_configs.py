@@ -31,7 +31,7 @@ def _oracle_eigs(sysm, kidx):
 @pytest.mark.gpu
 def test_diamond_all_kpoints_match_oracle(gpu_lib):
     from olcao_gb300 import api
-    sysm = S.CONFIGS["diamond"]()
+    sysm = S.SYSTEMS["diamond"]()
     ctx = api.Context(sysm)
     ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
     n = ctx.vale_dim
@@ -45,7 +45,7 @@ def test_diamond_all_kpoints_match_oracle(gpu_lib):
 @pytest.mark.gpu
 def test_graphite_mesh_slice_matches_oracle(gpu_lib):
     from olcao_gb300 import api
-    sysm = S.CONFIGS["graphite"]()
+    sysm = S.SYSTEMS["graphite"]()
     sysm.kpoints_abc = sysm.kpoints_abc[::16]          # 512 of the 8192 k-points
     ctx = api.Context(sysm)
     ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
@@ -62,7 +62,7 @@ def test_graphite_mesh_slice_matches_oracle(gpu_lib):
 def test_si8_full_mesh_mixed_and_fp64(gpu_lib):
     import torch
     from olcao_gb300 import api
-    sysm = S.CONFIGS["si8"]()
+    sysm = S.SYSTEMS["si8"]()
     ctx = api.Context(sysm)
     ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
     n, nk = ctx.vale_dim, ctx.nk

@@ -44,7 +44,7 @@ def _band_energy(w, nocc):
 def test_mixed_solver_matches_fp64_path(gpu_lib, name):
     import torch
     from olcao_gb300 import api
-    sysm = S.CONFIGS[name]()
+    sysm = S.SYSTEMS[name]()
     if name == "si8":
         sysm.kpoints_abc = sysm.kpoints_abc[:8]
     else:
@@ -79,7 +79,7 @@ def test_graph_replay_matches_direct_pass(gpu_lib):
     library."""
     import torch
     from olcao_gb300 import api
-    sysm = S.CONFIGS["si8"]()
+    sysm = S.SYSTEMS["si8"]()
     sysm.kpoints_abc = sysm.kpoints_abc[:16]
     ctx = api.Context(sysm)
     ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)

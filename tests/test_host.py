@@ -48,7 +48,7 @@ def test_library_rejects_bad_arguments_without_gpu():
     ("diamond", 10, 2, 216), ("si64", 832, 320, 64), ("graphite", 32, 0, 8192),
     ("si8", 104, 0, 512), ("quartz", 3159, 567, 9), ("si512", 6656, 2560, 9)])
 def test_synthetic_configs_have_the_stated_sizes(name, nv, nc, nk):
-    s = S.CONFIGS[name]()
+    s = S.SYSTEMS[name]()
     assert (s.vale_dim, s.core_dim, s.num_kpoints) == (nv, nc, nk)
     assert np.isclose(s.kpoint_weights().sum(), 2.0)
     # atoms do not collide
