@@ -280,6 +280,26 @@ def run_ours(args, world, rank, dist):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e = float(t.item())
 
+    # ---- next stage: valence density + traces of the last step's vectors ------
+    vrho = None
+    if rank == 0:
+        nocc_v = 2 * len(full.site_type) if args.config.startswith("si") else max(1, nstates // 4)
+        occ = np.zeros((nk, nstates))
+        occ[:, :nocc_v] = 2.0 / nk_total
+        eh = eig.cpu().numpy()
+        ctx.make_valence_rho(occ, vec, eh)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 3
+        for r in range(reps):
+            tr_v, en_v, _ = ctx.make_valence_rho(occ, vec, eh)
+        vrho = {"s_per_call": (time.perf_counter() - t0) / reps, "occupied_states": nocc_v,
+                "operators_traced": 3 + pd,
+                "operator_bytes_read": nk * (3 + pd) * (n * (n + 1) // 2) * 16,
+                "electrons": float(tr_v[0, 0]), "electron_energy_ha": float(en_v[0]),
+                "note": "makeValenceRho: rho = X diag(f) X^H (split-BF16, FP64-accurate) "
+                        "and its traces with S, NP, KE, V_j; not part of the timed step"}
+
     # ---- plain FP64 GPU path on the same step (accuracy and speed-up) ---------
     t_fp64 = None
     acc = None
@@ -370,6 +390,7 @@ def run_ours(args, world, rank, dist):
             "t_iter_fp64_gpu_s": t_fp64,
             "speedup_vs_fp64_gpu": (t_fp64 / (ms / 1e3)) if t_fp64 else None,
             "accuracy": acc,
+            "valence_rho": vrho,
             "stages": stages}
     print(json.dumps(line), flush=True)
 

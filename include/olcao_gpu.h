@@ -36,6 +36,8 @@
  *                              potential-dependent integrals recomputed
  *                              (src/olcao/secularEqn.F90:33-287,
  *                               src/uolcao/integrals.F90:2860-3605 fused form)
+ *   olc_make_valence_rho       makeValenceRho: density and operator traces
+ *                              (src/olcao/valeCharge.F90:34-420)
  */
 #ifndef OLCAO_GPU_H
 #define OLCAO_GPU_H
@@ -233,7 +235,8 @@ typedef enum {
   OLC_STAGE_ASSEMBLE = 4,
   OLC_STAGE_SOLVE = 5,
   OLC_STAGE_REFINE = 6,        /* mixed precision: split products + extraction */
-  OLC_NUM_STAGES = 7
+  OLC_STAGE_DENSITY = 7,       /* valence density and its traces               */
+  OLC_NUM_STAGES = 8
 } olc_stage_t;
 int olc_profile_enable(olc_context_t* ctx, int on);
 int olc_profile_reset(olc_context_t* ctx);
@@ -287,6 +290,30 @@ int olc_solve_zhegv_noalloc(int n, int nk, const double* packed_h, const double*
 int olc_write_setup_integrals(olc_context_t* ctx, const char* root);
 int olc_write_eigen(const char* root, int num_kpoints, int spin, int num_states, int vale_dim,
                     const double* eigenvalues, const double* vectors);
+
+/* makeValenceRho for one SCF iteration (src/olcao/valeCharge.F90:34-420;
+ * matrixElementMult, src/olcao/matrixSubs.F90:10-53): the valence density
+ *   rho_s(k) = sum_n f(n,k,s) x_n x_n^H
+ * over the states with sum_s |f(n,k,s)| >= 1e-8 (smallThresh), for spin = 2
+ * turned into (up + down, up - down), and its element-wise traces with the
+ * prepared operators, summed over k:
+ *   traces[3 + pot_dim, spin] = chargeDensityTrace, nucPotTrace,
+ *   kineticEnergyTrace, potRho(1..pot_dim) of each spin column
+ *   (column 1 total, column 2 difference when spin = 2).
+ * occupation[num_states, nk, spin] (structuredElectronPopulation: occupation
+ * times k-point weight) and eigenvalues[num_states, nk, spin] are HOST
+ * arrays; vectors[vale_dim, num_states, nk, spin] complex128 is DEVICE memory
+ * (olc_scf_iteration's vectors, one block per spin channel).
+ * electron_energy[spin] (HOST, may be NULL; needs eigenvalues) receives
+ * sum f * lambda per channel (electronEnergy).  rho_packed (DEVICE, may be
+ * NULL) receives packedValeValeRho of every k: [2, packed_len, nk, spin].
+ * Needs olc_scf_prepare; with OLC_FORM_FUSED the operators are recomputed
+ * one at a time (an integral pass each), with OLC_FORM_STORED the resident
+ * ones are read. */
+int olc_make_valence_rho(olc_context_t* ctx, int num_states, int spin,
+                         const double* occupation, const double* eigenvalues,
+                         const double* vectors, double* traces,
+                         double* electron_energy, double* rho_packed);
 
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the

@@ -16,6 +16,7 @@ this module                reference (src/olcao/...)
 ``solve_zhegv``            solveZHEGV         interfaces.F90:73-120
 ``scf_iteration``          secularEqnAllKP with the potential-dependent
                            integrals recomputed (fused form)
+``make_valence_rho``       makeValenceRho     valeCharge.F90:34-420
 =========================  ==================================================
 
 Device buffers are torch CUDA tensors (torch is only the allocator and
@@ -45,8 +46,10 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
            "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
-           "olc_split_zgemm", "olc_write_setup_integrals", "olc_write_eigen")
-STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve", "refine")
+           "olc_split_zgemm", "olc_write_setup_integrals", "olc_write_eigen",
+           "olc_make_valence_rho")
+STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve", "refine",
+          "density")
 
 _LIB: Optional[C.CDLL] = None
 
@@ -95,6 +98,7 @@ def lib() -> C.CDLL:
         L.olc_split_zgemm.argtypes = [vp, i32, i32, i32, dp, dp, dp]
         L.olc_write_setup_integrals.argtypes = [vp, C.c_char_p]
         L.olc_write_eigen.argtypes = [C.c_char_p, i32, i32, i32, i32, dp, dp]
+        L.olc_make_valence_rho.argtypes = [vp, i32, i32, dp, dp, dp, dp, dp, dp]
         L.olc_launch_count.restype = C.c_int64
         L.olc_launch_count.argtypes = []
         _LIB = L
@@ -336,3 +340,38 @@ class Context:
         _check(lib().olc_scf_iteration(self.h, cptr, precision, num_states,
                                        _ptr(eig_out), flags, _ptr(vectors)))
         return eig_out
+
+    def make_valence_rho(self, occupation, vectors, eigenvalues=None, rho: bool = False):
+        """makeValenceRho (valeCharge.F90:34-420) on the prepared operators.
+
+        occupation (and eigenvalues, optional) are host arrays [spin, nk,
+        num_states] or [nk, num_states] for spin 1: the reference's
+        structuredElectronPopulation, occupation times k-point weight.
+        vectors is a device complex128 tensor [spin, nk, num_states, n] (or
+        [nk, num_states, n]) as scf_iteration fills it.  Returns (traces
+        [spin, 3 + pot_dim] = chargeDensityTrace, nucPotTrace,
+        kineticEnergyTrace, potRho(1..pot_dim) per spin column (total,
+        difference); electronEnergy [spin] or None; packed rho tensor
+        [spin, nk, packed_len, 2] or None)."""
+        torch = self.torch
+        occ = np.ascontiguousarray(occupation, np.float64)
+        if occ.ndim == 2:
+            occ = occ[None]
+        spin, nk, ns = occ.shape
+        if nk != self.nk:
+            raise ValueError(f"occupation has {nk} k-points, the context {self.nk}")
+        if tuple(vectors.shape[-3:]) != (nk, ns, self.vale_dim) or vectors.numel() != spin * nk * ns * self.vale_dim:
+            raise ValueError(f"vectors shape {tuple(vectors.shape)} does not match occupation {occ.shape}")
+        if vectors.dtype != torch.complex128 or not vectors.is_contiguous():
+            raise ValueError("vectors must be a contiguous complex128 device tensor")
+        eig = None
+        if eigenvalues is not None:
+            eig = np.ascontiguousarray(eigenvalues, np.float64).reshape(occ.shape)
+        traces = np.zeros((spin, 3 + self.pot_dim))
+        energy = np.zeros(spin) if eig is not None else None
+        rp = (torch.zeros(spin, nk, self.packed_len, 2, dtype=torch.float64, device="cuda")
+              if rho else None)
+        _check(lib().olc_make_valence_rho(self.h, ns, spin, occ.ctypes.data, _ptr(eig),
+                                          vectors.data_ptr(), traces.ctypes.data, _ptr(energy),
+                                          _ptr(rp)))
+        return traces, energy, rp

@@ -329,4 +329,12 @@ int olc_write_eigen(const char* root, int num_kpoints, int spin, int num_states,
   return write_eigen(root, num_kpoints, spin, num_states, vale_dim, eigenvalues, vectors);
 }
 
+int olc_make_valence_rho(olc_context_t* ctx, int num_states, int spin, const double* occupation,
+                         const double* eigenvalues, const double* vectors, double* traces,
+                         double* electron_energy, double* rho_packed) {
+  if (!ctx) return fail(OLC_ERR_ARG, "olc_make_valence_rho: null context");
+  return make_valence_rho(ctx, num_states, spin, occupation, eigenvalues, vectors, traces, electron_energy,
+                          rho_packed);
+}
+
 }  // extern "C"

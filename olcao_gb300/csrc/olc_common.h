@@ -280,6 +280,11 @@ void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
 // status of a queued mixed solve (olc_mixed.cu)
 int mixed_check_info(olc_context* ctx);
 
+// valence density and its traces (olc_density.cu)
+int make_valence_rho(olc_context* ctx, int num_states, int spin, const double* occupation,
+                     const double* eigenvalues, const double* vectors, double* traces,
+                     double* electron_energy, double* rho_packed);
+
 // raw layout-identical dataset writer (olc_layout.cu)
 int write_setup_integrals(olc_context* ctx, const char* root);
 int write_eigen(const char* root, int nk, int spin, int num_states, int vale_dim, const double* eig,

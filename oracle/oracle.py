@@ -171,3 +171,66 @@ def zhegv(h_packed: np.ndarray, s_packed: np.ndarray, n: int, num_states: int):
         w[q] = ev[:num_states]
         vecs[q] = Z[:, :num_states]
     return w, vecs
+
+
+# ---- valence charge (the step after the eigen-solve) ------------------------
+SMALL_THRESH = 1.0e-8          # smallThresh, src/constants.f90:49
+
+
+def packed_index(n: int):
+    """(rows, cols) of the upper-packed order: column i, rows j <= i."""
+    cols = np.concatenate([np.full(i + 1, i) for i in range(n)])
+    rows = np.concatenate([np.arange(i + 1) for i in range(n)])
+    return rows, cols
+
+
+def matrix_element_mult(m1: np.ndarray, m2: np.ndarray) -> float:
+    """matrixElementMult (src/olcao/matrixSubs.F90:10-53) on packed [plen, 2]
+    arrays: off-diagonal elements contribute re*re + im*im, the diagonal only
+    re*re / 2, and the sum is doubled for the lower half."""
+    plen = m1.shape[0]
+    n = int(round((np.sqrt(8 * plen + 1) - 1) / 2))
+    diag = np.array([i * (i + 3) // 2 for i in range(n)])
+    prod = m1[:, 0] * m2[:, 0] + m1[:, 1] * m2[:, 1]
+    off = prod.sum() - prod[diag].sum()
+    return 2.0 * (off + (m1[diag, 0] * m2[diag, 0]).sum() / 2.0)
+
+
+def make_valence_rho(packed: Dict[str, np.ndarray], pot_dim: int, occupation: np.ndarray,
+                     eigenvalues: np.ndarray, vectors: np.ndarray):
+    """makeValenceRho (src/olcao/valeCharge.F90:172-395) for stored operators.
+
+    occupation, eigenvalues: [spin, nk, num_states] (the reference's
+    (numStates, numKPoints, spin) in memory order); vectors [spin, nk,
+    num_states, n] complex (valeVale(:, state) per k).  Per k: the states
+    with sum_s |f| >= smallThresh (:234) add f * lambda to the electron
+    energy and f x x^H to rho's upper triangle (zher, :240); rho is packed,
+    for spin 2 turned into (up + down, up - down) (:307-313), and traced with
+    S, NP, KE and every V_j (:321-395).
+
+    Returns (traces [spin, 3 + pot_dim] = charge, nuclear, kinetic, potRho,
+    electron energy [spin], packed rho [spin, nk, plen, 2])."""
+    spin, nk, ns = occupation.shape
+    n = vectors.shape[-1]
+    rows, cols = packed_index(n)
+    traces = np.zeros((spin, 3 + pot_dim))
+    energy = np.zeros(spin)
+    rho_packed = np.zeros((spin, nk, rows.size, 2))
+    names = ["S", "NP", "KE"] + [f"V{j}" for j in range(pot_dim)]
+    for k in range(nk):
+        keep = [j for j in range(ns) if np.abs(occupation[:, k, j]).sum() >= SMALL_THRESH]
+        for j in keep:
+            energy += occupation[:, k, j] * eigenvalues[:, k, j]
+        pk = []
+        for s in range(spin):
+            X = vectors[s, k][keep].T                      # [n, nocc]
+            R = (X * occupation[s, k, keep][None, :]) @ X.conj().T
+            v = R[rows, cols]
+            pk.append(np.stack([v.real, v.imag], -1))
+        if spin == 2:
+            pk = [pk[0] + pk[1], pk[0] - pk[1]]
+        for s in range(spin):
+            rho_packed[s, k] = pk[s]
+            for t, name in enumerate(names):
+                traces[s, t] += matrix_element_mult(packed[name][k], pk[s])
+    return traces, energy, rho_packed
