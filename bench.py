@@ -65,7 +65,44 @@ def parse():
     p.add_argument("--cpu-sample-k", type=int, default=2)
     p.add_argument("--nk", type=int, default=0,
                    help="profiling runs only: keep the first NK k-points")
+    p.add_argument("--k-stride", type=int, default=1,
+                   help="with --valence-rho-only: keep every K_STRIDE-th k-point")
+    p.add_argument("--valence-rho-only", action="store_true",
+                   help="profiling runs only: prepare, one pass with vectors, then two "
+                        "olc_make_valence_rho calls between cudaProfilerStart/Stop")
     return p.parse_args()
+
+
+def run_valence_rho_only(args):
+    """The density step alone, for ncu (--profile-from-start off) captures."""
+    import torch
+    from olcao_gb300 import api
+    from olcao_gb300 import system as S
+    sysm = S.SYSTEMS[args.config]()
+    sysm.kpoints_abc = sysm.kpoints_abc[::args.k_stride]
+    if args.nk > 0:
+        sysm.kpoints_abc = sysm.kpoints_abc[:args.nk]
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n, nk, pd = ctx.vale_dim, ctx.nk, ctx.pot_dim
+    prec = api.PREC_MIXED if args.precision == "mixed" else api.PREC_FP64
+    vec = torch.zeros(nk, n, n, dtype=torch.complex128, device="cuda")
+    w = ctx.scf_iteration(sysm.pot_coeffs, n, precision=prec, vectors=vec)
+    nocc = 2 * len(sysm.site_type) if args.config.startswith("si") else max(1, n // 4)
+    occ = np.zeros((nk, n))
+    occ[:, :nocc] = 2.0 / nk
+    ctx.make_valence_rho(occ, vec, w)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        tr, en, _ = ctx.make_valence_rho(occ, vec, w)
+    dt = (time.perf_counter() - t0) / 2
+    torch.cuda.profiler.stop()
+    plen = n * (n + 1) // 2
+    print(json.dumps({"workload": f"{args.config}, {nk} k (stride {args.k_stride}), {nocc} occupied",
+                      "s_per_call": dt, "electrons": float(tr[0, 0]),
+                      "trace_bytes_per_launch": nk * plen * 16 * (3 + pd + 1)}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -410,6 +447,8 @@ def main():
         dist = td
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.valence_rho_only:
+        run_valence_rho_only(args)
     else:
         run_ours(args, world, rank, dist)
     if dist:

@@ -35,6 +35,7 @@ namespace {
 constexpr double kSmallThresh = 1.0e-8;   // smallThresh, src/constants.f90:49
 constexpr int kTraceThreads = 256;
 constexpr int kTraceEpt = 4;               // packed elements per thread per tile
+constexpr int kTraceChunk = 24;            // operators per trace launch (48 KB of accumulators)
 
 int grid_of(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
@@ -103,19 +104,20 @@ __global__ void pack_rho_kernel(const double* __restrict__ full, int n, int nk, 
 // Element-wise traces of rho against nt operators.  Operator 0 is the full
 // S [nk][n][n] when sfull != nullptr; the others are packed terms
 // [nt'][nk][plen][2] (term stride tstride doubles).  Block (b, k) walks tiles
-// b, b + gridDim.x, ... of k's packed index range; each warp keeps its
-// running sums in shared memory (one row of nt) and the block writes
-// partial[(k * gridDim.x + b) * nt + t].
+// b, b + gridDim.x, ... of k's packed index range.  Every thread keeps one
+// running sum per operator in shared memory (sacc[t][thread]), so the inner
+// loop has no cross-thread traffic; the block reduces them once at the end
+// and writes partial[(k * gridDim.x + b) * nt + t].  Each pass over a tile
+// has the loads of two operators in flight.
 __global__ void __launch_bounds__(kTraceThreads) trace_kernel(
     const double* __restrict__ rho, const double* __restrict__ sfull, const double* __restrict__ terms,
     long long tstride, int nt, int n, long long plen, double* __restrict__ partial) {
-  extern __shared__ double sacc[];           // [warps][nt]
-  const int k = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
-  for (int q = threadIdx.x; q < nwarps * nt; q += blockDim.x) sacc[q] = 0.0;
-  __syncthreads();
+  extern __shared__ double sacc[];           // [nt][kTraceThreads]
+  const int k = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int t = 0; t < nt; ++t) sacc[t * kTraceThreads + tid] = 0.0;
   const size_t nn = (size_t)n * n;
-  const double* rk = rho + 2 * (size_t)k * nn;
+  const double2* rk = reinterpret_cast<const double2*>(rho) + (size_t)k * nn;
+  const double2* sk = sfull ? reinterpret_cast<const double2*>(sfull) + (size_t)k * nn : nullptr;
   const int npk = sfull ? 1 : 0;
   const long long tile = (long long)kTraceThreads * kTraceEpt;
   for (long long base = (long long)blockIdx.x * tile; base < plen; base += (long long)gridDim.x * tile) {
@@ -124,46 +126,67 @@ __global__ void __launch_bounds__(kTraceThreads) trace_kernel(
     long long pr[kTraceEpt];
 #pragma unroll
     for (int e = 0; e < kTraceEpt; ++e) {
-      const long long r = base + (long long)e * kTraceThreads + threadIdx.x;
-      pr[e] = r;
-      wr[e] = wi[e] = 0.0;
-      foff[e] = 0;
-      if (r < plen) {
-        int i = (int)((sqrt(8.0 * (double)r + 1.0) - 1.0) * 0.5);
-        while ((long long)i * (i + 1) / 2 > r) --i;
-        while ((long long)(i + 1) * (i + 2) / 2 <= r) ++i;
-        const int j = (int)(r - (long long)i * (i + 1) / 2);
-        foff[e] = (size_t)i * n + j;
-        const double xr = rk[2 * foff[e]], xi = rk[2 * foff[e] + 1];
-        // the diagonal counts once and only its real part; off-diagonal
-        // elements stand for themselves and their mirror image
-        wr[e] = (i == j) ? xr : 2.0 * xr;
-        wi[e] = (i == j) ? 0.0 : 2.0 * xi;
-      }
+      const long long r = base + (long long)e * kTraceThreads + tid;
+      pr[e] = r < plen ? r : plen - 1;       // clamped: in bounds, weight 0
+      int i = (int)((sqrtf(8.0f * (float)pr[e] + 1.0f) - 1.0f) * 0.5f);
+      while ((long long)i * (i + 1) / 2 > pr[e]) --i;
+      while ((long long)(i + 1) * (i + 2) / 2 <= pr[e]) ++i;
+      const int j = (int)(pr[e] - (long long)i * (i + 1) / 2);
+      foff[e] = (size_t)i * n + j;
+      const double2 x = rk[foff[e]];
+      // the diagonal counts once and only its real part; off-diagonal
+      // elements stand for themselves and their mirror image
+      const double g = r < plen ? (i == j ? 1.0 : 2.0) : 0.0;
+      wr[e] = g * x.x;
+      wi[e] = (i == j) ? 0.0 : g * x.y;
     }
-    for (int t = 0; t < nt; ++t) {
-      double acc = 0.0;
-      if (t < npk) {
-        const double* sk = sfull + 2 * (size_t)k * nn;
+    int t = 0;
+    if (npk) {
+      double a = 0.0;
 #pragma unroll
-        for (int e = 0; e < kTraceEpt; ++e)
-          if (pr[e] < plen) acc += sk[2 * foff[e]] * wr[e] + sk[2 * foff[e] + 1] * wi[e];
-      } else {
-        const double* tk = terms + (size_t)(t - npk) * tstride + 2 * (size_t)k * plen;
-#pragma unroll
-        for (int e = 0; e < kTraceEpt; ++e)
-          if (pr[e] < plen) acc += tk[2 * pr[e]] * wr[e] + tk[2 * pr[e] + 1] * wi[e];
+      for (int e = 0; e < kTraceEpt; ++e) {
+        const double2 v = sk[foff[e]];
+        a += v.x * wr[e] + v.y * wi[e];
       }
+      sacc[tid] += a;
+      t = 1;
+    }
+    for (; t + 1 < nt; t += 2) {
+      const double2* t0 = reinterpret_cast<const double2*>(terms + (size_t)(t - npk) * tstride) + (size_t)k * plen;
+      const double2* t1 = reinterpret_cast<const double2*>(terms + (size_t)(t + 1 - npk) * tstride) + (size_t)k * plen;
+      double2 v0[kTraceEpt], v1[kTraceEpt];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-      if (lane == 0) sacc[warp * nt + t] += acc;
+      for (int e = 0; e < kTraceEpt; ++e) {
+        v0[e] = t0[pr[e]];
+        v1[e] = t1[pr[e]];
+      }
+      double a0 = 0.0, a1 = 0.0;
+#pragma unroll
+      for (int e = 0; e < kTraceEpt; ++e) {
+        a0 += v0[e].x * wr[e] + v0[e].y * wi[e];
+        a1 += v1[e].x * wr[e] + v1[e].y * wi[e];
+      }
+      sacc[t * kTraceThreads + tid] += a0;
+      sacc[(t + 1) * kTraceThreads + tid] += a1;
+    }
+    if (t < nt) {
+      const double2* t0 = reinterpret_cast<const double2*>(terms + (size_t)(t - npk) * tstride) + (size_t)k * plen;
+      double a0 = 0.0;
+#pragma unroll
+      for (int e = 0; e < kTraceEpt; ++e) {
+        const double2 v = t0[pr[e]];
+        a0 += v.x * wr[e] + v.y * wi[e];
+      }
+      sacc[t * kTraceThreads + tid] += a0;
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-    double s = 0.0;
-    for (int w = 0; w < nwarps; ++w) s += sacc[w * nt + t];
-    partial[((size_t)k * gridDim.x + blockIdx.x) * nt + t] = s;
+  for (int t = warp; t < nt; t += kTraceThreads / 32) {
+    double a = 0.0;
+    for (int q = lane; q < kTraceThreads; q += 32) a += sacc[t * kTraceThreads + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) partial[((size_t)k * gridDim.x + blockIdx.x) * nt + t] = a;
   }
 }
 
@@ -201,21 +224,24 @@ struct Scratch {
   }
 };
 
-// Traces of rho (all k) against nt operators into out[nt] (device).
+// Traces of rho (all k) against nt operators into out[nt] (device), in
+// chunks of at most kTraceChunk operators (per-thread accumulators of one
+// chunk fill 48 KB of shared memory).
 int launch_traces(olc_context* ctx, const double* rho, const double* sfull, const double* terms,
                   long long tstride, int nt, double* partial, int bx, double* out) {
   const int n = ctx->dims.vale_dim, nk = ctx->dims.num_kpoints;
   const long long plen = ctx->dims.packed_len;
-  const size_t smem = sizeof(double) * (kTraceThreads / 32) * nt;
-  if (smem > 48 * 1024) {
-    int st = cuda_check(cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                        "trace smem");
-    if (st) return st;
+  StageScope scope(ctx, OLC_STAGE_DENSITY, 0);
+  for (int t0 = 0; t0 < nt; t0 += kTraceChunk) {
+    const int c = std::min(kTraceChunk, nt - t0);
+    const bool with_s = sfull && t0 == 0;
+    const double* tp = terms ? terms + (size_t)(t0 - (sfull && t0 > 0 ? 1 : 0)) * tstride : nullptr;
+    const size_t smem = sizeof(double) * kTraceThreads * c;
+    trace_kernel<<<dim3(bx, nk), kTraceThreads, smem, ctx->stream>>>(rho, with_s ? sfull : nullptr, tp, tstride, c,
+                                                                      n, plen, partial);
+    reduce_partials_kernel<<<c, 256, 0, ctx->stream>>>(partial, bx * nk, c, out + t0);
+    scope.add_launches(2);
   }
-  StageScope scope(ctx, OLC_STAGE_DENSITY, 2);
-  trace_kernel<<<dim3(bx, nk), kTraceThreads, smem, ctx->stream>>>(rho, sfull, terms, tstride, nt, n, plen,
-                                                                    partial);
-  reduce_partials_kernel<<<nt, 256, 0, ctx->stream>>>(partial, bx * nk, nt, out);
   return cuda_check(cudaGetLastError(), "trace kernels");
 }
 
