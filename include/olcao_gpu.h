@@ -21,9 +21,9 @@
  *                               src/olcao/kpoints.f90:286-310,
  *                               src/olcao/basis.f90:55-243,
  *                               src/olcao/gaussRelations.f90:64-278)
- *   olc_gauss_overlap          gaussOverlapOL / KE / NP / EP (+ saveCurrentPair)
+ *   olc_gauss_overlap          gaussOverlapOL / KE / MV / NP / EP (+ saveCurrentPair)
  *                              (src/olcao/integrals.F90:81-486, 490-900,
- *                               1324-1715, 1719-2122;
+ *                               904-1320, 1324-1715, 1719-2122;
  *                               src/olcao/intgSaving.F90:56-550)
  *   olc_ortho_pack             orthoOL / ortho(opCode) + makeValeVale packing
  *                              (src/olcao/integrals.F90:2601-2853,
@@ -106,6 +106,10 @@ typedef struct {
   int32_t num_kpoints;
   const double*  kpoints_abc;             /* [3*num_kpoints] fractional       */
   double basis_fn_thresh;                 /* BASIS_FN convergence, e.g. 1e-16 */
+  int32_t rel;                            /* 1: scalar-relativistic, the mass-
+                                             velocity term joins H (the
+                                             reference's rel, OLCAO_Setup.f90:
+                                             142-144); 0: non-relativistic  */
 } olc_system_t;
 
 /* Integral operators (the reference's opCode values, integrals.F90:2710-2853). */
@@ -114,7 +118,9 @@ typedef enum {
   OLC_OP_KINETIC = 2,     /* gaussOverlapKE -> atomKEOverlap                  */
   OLC_OP_NUCLEAR = 3,     /* gaussOverlapNP -> atomNucOverlap                 */
   OLC_OP_ELECPOT = 4,     /* gaussOverlapEP -> atomPotOverlap(term)           */
-  OLC_OP_HAMILTONIAN = 6  /* KE + NP + sum_j c_j V_j in one pass (fused form) */
+  OLC_OP_MASSVEL = 5,     /* gaussOverlapMV -> atomMVOverlap (with the driver's
+                             minus sign, integrals.F90:1222-1236)            */
+  OLC_OP_HAMILTONIAN = 6  /* KE + NP (+ MV) + sum_j c_j V_j in one pass (fused form) */
 } olc_op_t;
 
 typedef enum {
@@ -166,9 +172,10 @@ int olc_ortho_pack(olc_context_t* ctx, int is_overlap, double* vv,
                    const double* cv, const double* cc, const double* s_cv,
                    double* packed);
 
-/* H(k) packed = NP + KE + sum_j c_j V_j with the reference's rule that a
- * zero coefficient adds the term with factor 1 (matrixSubs.F90:278-282).
- * terms[nterm] are DEVICE pointers to packed[2, packed_len, nk] arrays. */
+/* H(k) packed = NP + KE (+ MV) + sum_j c_j V_j with the reference's rule
+ * that a zero coefficient adds the term with factor 1 (matrixSubs.F90:
+ * 278-282).  terms[nterm] are DEVICE pointers to packed[2, packed_len, nk]
+ * arrays, coeffs[nterm] their multipliers. */
 int olc_assemble_hamiltonian(olc_context_t* ctx, const double* const* terms,
                              const double* coeffs, int nterm, double* packed_h);
 
@@ -197,8 +204,9 @@ typedef enum {
                                      capture is refused)                      */
 
 /* Set-up of the iteration-invariant parts of the SCF pass: S(k) orthogonalised,
- * H0 = ortho(KE + NP), and for OLC_FORM_STORED every orthogonalised, packed
- * V_j.  Must precede olc_scf_iteration. */
+ * H0 = ortho(KE + NP (+ MV when rel = 1)), and for OLC_FORM_STORED every
+ * orthogonalised, packed operator (NP, KE, MV when rel = 1, V_j) kept apart.
+ * Must precede olc_scf_iteration. */
 int olc_scf_prepare(olc_context_t* ctx, int precision, int form);
 
 /* One SCF-iteration pass of the hot path (secularEqnAllKP): H(k) built with
@@ -276,8 +284,9 @@ int olc_solve_zhegv_noalloc(int n, int nk, const double* packed_h, const double*
  *
  * olc_write_setup_integrals replaces the integral writes of setup-temp.hdf5
  * (hdf5SetupIntg.F90:86-222; integrals.F90:2693, 2826-2840): for every k,
- * /atomIntgGroup/atomOverlap/%07d, atomKEOverlap/%07d, atomNucOverlap/%07d
- * and atomPotOverlap/%07d/%07d (k, term), each (2, vale_dim(vale_dim+1)/2)
+ * /atomIntgGroup/atomOverlap/%07d, atomKEOverlap/%07d, atomNucOverlap/%07d,
+ * atomMVOverlap/%07d (rel = 1) and atomPotOverlap/%07d/%07d (k, term), each
+ * (2, vale_dim(vale_dim+1)/2)
  * upper-packed orthogonalised values.  Needs olc_scf_prepare(...,
  * OLC_FORM_STORED).
  *
@@ -297,9 +306,9 @@ int olc_write_eigen(const char* root, int num_kpoints, int spin, int num_states,
  * over the states with sum_s |f(n,k,s)| >= 1e-8 (smallThresh), for spin = 2
  * turned into (up + down, up - down), and its element-wise traces with the
  * prepared operators, summed over k:
- *   traces[3 + pot_dim, spin] = chargeDensityTrace, nucPotTrace,
- *   kineticEnergyTrace, potRho(1..pot_dim) of each spin column
- *   (column 1 total, column 2 difference when spin = 2).
+ *   traces[3 + rel + pot_dim, spin] = chargeDensityTrace, nucPotTrace,
+ *   kineticEnergyTrace, massVelocityTrace (rel = 1 only), potRho(1..pot_dim)
+ *   of each spin column (column 1 total, column 2 difference when spin = 2).
  * occupation[num_states, nk, spin] (structuredElectronPopulation: occupation
  * times k-point weight) and eigenvalues[num_states, nk, spin] are HOST
  * arrays; vectors[vale_dim, num_states, nk, spin] complex128 is DEVICE memory
@@ -318,7 +327,7 @@ int olc_make_valence_rho(olc_context_t* ctx, int num_states, int spin,
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the
  * device.  kind: 1 overlap2CIntg, 2 kinetic2CIntg, 3 nuclear3CIntg,
- * 4 electron3CIntg.  in[n*12] = (a1,a2,a3,Ax,Ay,Az,Bx,By,Bz,Cx,Cy,Cz),
+ * 4 electron3CIntg, 5 massvel2CIntg.  in[n*12] = (a1,a2,a3,Ax,Ay,Az,Bx,By,Bz,Cx,Cy,Cz),
  * lmalpha[n*2]; out[n*256] = sh(16,16) column-major (host arrays). */
 int olc_primitive_batch(int kind, int n, const double* in,
                         const int32_t* lmalpha, double* out);

@@ -9,6 +9,7 @@ this module                reference (src/olcao/...)
                            Factors, renormalizeBasis, makeAlpha*Dist
 ``gauss_overlap(OL)``      gaussOverlapOL     integrals.F90:81-486
 ``gauss_overlap(KE)``      gaussOverlapKE     integrals.F90:490-900
+``gauss_overlap(MV)``      gaussOverlapMV     integrals.F90:904-1320
 ``gauss_overlap(NP)``      gaussOverlapNP     integrals.F90:1324-1715
 ``gauss_overlap(EP, j)``   gaussOverlapEP     integrals.F90:1719-2122
 ``ortho_pack``             orthoOL / ortho    integrals.F90:2601-2853
@@ -35,7 +36,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libolcao_gb300.so")
 
-OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT, OP_HAMILTONIAN = 1, 2, 3, 4, 6
+OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT, OP_MASSVEL, OP_HAMILTONIAN = 1, 2, 3, 4, 5, 6
 PREC_FP64, PREC_MIXED = 0, 1
 FORM_FUSED, FORM_STORED = 0, 1
 ITER_EIG_DEVICE, ITER_COEFF_DEVICE, ITER_GRAPH = 1, 2, 4
@@ -186,6 +187,7 @@ class Context:
         self.h = h
         d = Dims()
         _check(lib().olc_get_dims(h, C.byref(d)))
+        self.rel = int(getattr(system, "rel", 0))
         self.vale_dim, self.core_dim = d.vale_dim, d.core_dim
         self.pot_dim, self.nk = d.pot_dim, d.num_kpoints
         self.num_cells, self.num_pair_tasks = d.num_cells, d.num_pair_tasks
@@ -257,7 +259,8 @@ class Context:
         """OLCAOsetup's stored integrals: packed, orthogonalised S, KE, NP, V_j."""
         vvS, cvS, ccS = self.gauss_overlap(OP_OVERLAP)
         out = {"S": self.ortho_pack(True, vvS.clone(), cvS, ccS, cvS)}
-        for name, op in (("KE", OP_KINETIC), ("NP", OP_NUCLEAR)):
+        ops = (("KE", OP_KINETIC), ("NP", OP_NUCLEAR)) + ((("MV", OP_MASSVEL),) if self.rel else ())
+        for name, op in ops:
             vv, cv, cc = self.gauss_overlap(op)
             out[name] = self.ortho_pack(False, vv, cv, cc, cvS)
         terms = range(self.pot_dim) if terms is None else terms
@@ -267,8 +270,9 @@ class Context:
         return out
 
     def assemble_hamiltonian(self, packed: Dict[str, object], coeffs) -> object:
-        terms = [packed["NP"], packed["KE"]] + [packed[f"V{j}"] for j in range(self.pot_dim)]
-        co = np.concatenate([[1.0, 1.0], np.asarray(coeffs, np.float64)])
+        fixed = [packed["NP"], packed["KE"]] + ([packed["MV"]] if "MV" in packed else [])
+        terms = fixed + [packed[f"V{j}"] for j in range(self.pot_dim)]
+        co = np.concatenate([np.ones(len(fixed)), np.asarray(coeffs, np.float64)])
         ptrs = (C.c_void_p * len(terms))(*[t.data_ptr() for t in terms])
         out = self.torch.empty_like(packed["NP"])
         _check(lib().olc_assemble_hamiltonian(self.h, C.cast(ptrs, C.c_void_p),
@@ -349,10 +353,10 @@ class Context:
         structuredElectronPopulation, occupation times k-point weight.
         vectors is a device complex128 tensor [spin, nk, num_states, n] (or
         [nk, num_states, n]) as scf_iteration fills it.  Returns (traces
-        [spin, 3 + pot_dim] = chargeDensityTrace, nucPotTrace,
-        kineticEnergyTrace, potRho(1..pot_dim) per spin column (total,
-        difference); electronEnergy [spin] or None; packed rho tensor
-        [spin, nk, packed_len, 2] or None)."""
+        [spin, 3 + rel + pot_dim] = chargeDensityTrace, nucPotTrace,
+        kineticEnergyTrace, massVelocityTrace (rel = 1 only), potRho(1..pot_dim)
+        per spin column (total, difference); electronEnergy [spin] or None;
+        packed rho tensor [spin, nk, packed_len, 2] or None)."""
         torch = self.torch
         occ = np.ascontiguousarray(occupation, np.float64)
         if occ.ndim == 2:
@@ -367,7 +371,7 @@ class Context:
         eig = None
         if eigenvalues is not None:
             eig = np.ascontiguousarray(eigenvalues, np.float64).reshape(occ.shape)
-        traces = np.zeros((spin, 3 + self.pot_dim))
+        traces = np.zeros((spin, 3 + self.rel + self.pot_dim))
         energy = np.zeros(spin) if eig is not None else None
         rp = (torch.zeros(spin, nk, self.packed_len, 2, dtype=torch.float64, device="cuda")
               if rho else None)

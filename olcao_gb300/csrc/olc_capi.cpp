@@ -222,9 +222,10 @@ int olc_gauss_overlap(olc_context_t* ctx, int op, int term, const double* coeffs
     cudaMemcpyAsync(dco, c.data(), sizeof(double) * pd, cudaMemcpyHostToDevice, ctx->stream);
     st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, precision, false);
     if (!st) st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, precision, true);
+    if (!st && ctx->rel) st = run_primitives(ctx, OLC_OP_MASSVEL, 0, nullptr, precision, true);
     if (!st) st = run_primitives(ctx, OLC_OP_ELECPOT, 0, dco, precision, true);
     cudaFreeAsync(dco, ctx->stream);
-  } else if (op >= OLC_OP_OVERLAP && op <= OLC_OP_ELECPOT) {
+  } else if (op >= OLC_OP_OVERLAP && op <= OLC_OP_MASSVEL) {
     if (op == OLC_OP_ELECPOT && (term < 0 || term >= ctx->dims.pot_dim))
       return fail(OLC_ERR_ARG, "potential term out of range");
     st = run_primitives(ctx, op, term, nullptr, precision, false);

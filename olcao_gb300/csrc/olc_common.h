@@ -144,10 +144,11 @@ struct olc_context {
   int64_t block_stride = 0;        // doubles per task block (MS*MS)
   int max_states = 0;
   // cached iteration-invariant data (olc_scf_prepare)
+  int rel = 0;                     // 1: mass-velocity term in H (scalar relativistic)
   bool prepared = false;
   int prep_precision = 0;
   int prep_form = 0;
-  double* d_terms = nullptr;       // stored form: packed NP, KE, V_j [2+pd][nk][plen][2]
+  double* d_terms = nullptr;       // stored form: packed NP, KE, (MV), V_j [2+rel+pd][nk][plen][2]
   double* d_scv = nullptr;         // S core-vale  [nk][nv][nc] complex
   double* d_h0 = nullptr;          // ortho(KE + NP) full upper [nk][nv][nv] complex
   double* d_chol = nullptr;        // Cholesky factor of ortho'd S, [nk][nv][nv]

@@ -6,7 +6,7 @@
 // triangle of rho one zher per occupied state (valeCharge.F90:232-241),
 // packs it (packMatrix), turns the two channels into total and difference
 // when spin = 2 (:307-313), and forms for every stored operator T (overlap,
-// nuclear, kinetic, each potential term)
+// nuclear, kinetic, mass velocity when rel = 1, each potential term)
 //     sum_{j<i} 2 (Re T_ji Re rho_ji + Im T_ji Im rho_ji) + sum_i Re T_ii Re rho_ii
 // accumulated over k (:321-395).
 //
@@ -259,7 +259,8 @@ int make_valence_rho(olc_context* ctx, int num_states, int spin, const double* o
     return fail(OLC_ERR_ARG, "olc_make_valence_rho: occupation, vectors and traces are required");
   if (electron_energy && !eigenvalues)
     return fail(OLC_ERR_ARG, "olc_make_valence_rho: electron_energy needs eigenvalues");
-  const int nt = 3 + pd;
+  const int nfix = 2 + ctx->rel;            // NP, KE (, MV) ahead of the V_j
+  const int nt = 1 + nfix + pd;
   const size_t nn = (size_t)n * n;
   auto occ = [&](int s, int k, int j) { return occupation[j + (size_t)num_states * (k + (size_t)nk * s)]; };
 
@@ -344,7 +345,7 @@ int make_valence_rho(olc_context* ctx, int num_states, int spin, const double* o
   if ((rc = sc.get(&partial, sizeof(double) * (size_t)bx * nk * nt, "malloc partial traces"))) return rc;
   const long long tstride = 2 * plen * nk;
   if (ctx->prep_form == OLC_FORM_STORED && ctx->d_terms) {
-    // d_terms holds NP, KE, V_j in the trace order of the reference
+    // d_terms holds NP, KE, (MV,) V_j in the trace order of the reference
     for (int s = 0; s < spin; ++s)
       if ((rc = launch_traces(ctx, rho + 2 * (size_t)s * nn * nk, ctx->d_chol, ctx->d_terms, tstride, nt, partial,
                               bx, dtr + (size_t)s * nt))) return rc;
@@ -357,10 +358,10 @@ int make_valence_rho(olc_context* ctx, int num_states, int spin, const double* o
     for (int s = 0; s < spin; ++s)
       if ((rc = launch_traces(ctx, rho + 2 * (size_t)s * nn * nk, ctx->d_chol, nullptr, 0, 1, partial, bx,
                               dtr + (size_t)s * nt))) return rc;
-    const int ops[2] = {OLC_OP_NUCLEAR, OLC_OP_KINETIC};
-    for (int t = 0; t < 2 + pd; ++t) {
-      const int op = t < 2 ? ops[t] : OLC_OP_ELECPOT;
-      if ((rc = run_primitives(ctx, op, t < 2 ? 0 : t - 2, nullptr, OLC_PREC_FP64, false))) return rc;
+    const int ops[3] = {OLC_OP_NUCLEAR, OLC_OP_KINETIC, OLC_OP_MASSVEL};
+    for (int t = 0; t < nfix + pd; ++t) {
+      const int op = t < nfix ? ops[t] : OLC_OP_ELECPOT;
+      if ((rc = run_primitives(ctx, op, t < nfix ? 0 : t - nfix, nullptr, OLC_PREC_FP64, false))) return rc;
       if ((rc = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return rc;
       if ((rc = ortho_pack(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv, tmp, nullptr)))
         return rc;

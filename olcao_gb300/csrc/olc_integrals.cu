@@ -2,7 +2,8 @@
 //
 // Stage 1 (primitive kernels, one thread per alpha-pair item, one launch per
 //   angular class so a warp runs one straight-line recurrence):  the reference's
-//   alpha loop body -- overlap2CIntg / kinetic2CIntg (integrals.F90:312-416)
+//   alpha loop body -- overlap2CIntg / kinetic2CIntg / massvel2CIntg
+//   (integrals.F90:312-416, 1150-1236)
 //   and the third-centre sums of nuclearPE / electronicPE (integrals.F90:
 //   2275-2598) -- producing the harmonic block sh(lm1, lm2) of each item in
 //   a scratch buffer.
@@ -135,6 +136,10 @@ __global__ void __launch_bounds__(128) prim_kernel(SysView v, PrimArgs a) {
     add_overlap<L1, L2>(g.a1, g.a2, g.A, g.B, 1.0, cart);
   } else if constexpr (OP == OLC_OP_KINETIC) {
     add_kinetic<L1, L2>(g.a1, g.a2, g.A, g.B, 1.0, cart);
+  } else if constexpr (OP == OLC_OP_MASSVEL) {
+    // gaussOverlapMV accumulates the primitive with a minus sign
+    // (integrals.F90:1228-1236): the mass-velocity term lowers H
+    add_massvel<L1, L2>(g.a1, g.a2, g.A, g.B, -1.0, cart);
   } else {
     // centre of the alpha-pair overlap (alphaCenter, gaussRelations.f90:122)
     const double al = elem_alpha(v, g.e1, g.ia1), ak = elem_alpha(v, g.e2, g.ia2);
@@ -244,6 +249,7 @@ int run_primitives(olc_context* ctx, int op, int term, const double* coeffs, int
     switch (op) {
       case OLC_OP_OVERLAP: st = launch_class<OLC_OP_OVERLAP, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
       case OLC_OP_KINETIC: st = launch_class<OLC_OP_KINETIC, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
+      case OLC_OP_MASSVEL: st = launch_class<OLC_OP_MASSVEL, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
       case OLC_OP_NUCLEAR: st = launch_class<OLC_OP_NUCLEAR, 0>(ctx, cls, nullptr, -1, 0, accumulate); break;
       case OLC_OP_ELECPOT:
         if (far32) {
@@ -454,6 +460,7 @@ __device__ void prim_one(int kind, const double* in, double* out) {
   if (kind == 1) add_overlap<L1, L2>(in[0], in[1], A, B, 1.0, cart);
   else if (kind == 2) add_kinetic<L1, L2>(in[0], in[1], A, B, 1.0, cart);
   else if (kind == 3) add_nuclear<L1, L2>(in[0], in[1], in[2], A, B, C, 1.0, cart);
+  else if (kind == 5) add_massvel<L1, L2>(in[0], in[1], A, B, 1.0, cart);
   else {
     double d2 = 0.0;
     for (int c = 0; c < 3; ++c) d2 += (A[c] - B[c]) * (A[c] - B[c]);
@@ -489,7 +496,7 @@ __global__ void prim_batch_kernel(int kind, int n, const double* in, const int32
 
 int primitive_batch_device(int kind, int n, const double* in, const int32_t* lmalpha,
                            double* out) {
-  if (kind < 1 || kind > 4 || n < 0) return fail(OLC_ERR_ARG, "olc_primitive_batch: bad kind");
+  if (kind < 1 || kind > 5 || n < 0) return fail(OLC_ERR_ARG, "olc_primitive_batch: bad kind");
   for (int i = 0; i < n; ++i) {
     for (int s = 0; s < 2; ++s) {
       int l = lmalpha[2 * i + s];

@@ -2,7 +2,7 @@
 //
 // The reference stores the orthogonalised, packed integrals of every k in
 // setup-temp.hdf5 (hdf5SetupIntg.F90:86-222: groups
-// /atomIntgGroup/{atomOverlap,atomKEOverlap,atomNucOverlap}/%07d(k) and
+// /atomIntgGroup/{atomOverlap,atomKEOverlap,atomMVOverlap,atomNucOverlap}/%07d(k) and
 // /atomIntgGroup/atomPotOverlap/%07d(k)/%07d(term), each a (2, n(n+1)/2)
 // binary64 dataset) and the eigen-solutions in main-temp.hdf5
 // (hdf5MainEval.f90:60-81: /eigenValues/%07d%07d(k, spin), (numStates);
@@ -112,24 +112,27 @@ int write_setup_integrals(olc_context* ctx, const char* root) {
   pack_upper_kernel<<<(int)std::min<size_t>((plen * nk + 255) / 256, 152 * 16), 256, 0, ctx->stream>>>(
       ctx->d_chol, nv, nk, dS);
   count_launch();
-  std::vector<double> hS(plen2), hT(plen2 * (2 + pd));
+  const int nfix = 2 + ctx->rel;
+  std::vector<double> hS(plen2), hT(plen2 * (nfix + pd));
   st = cuda_check(cudaMemcpyAsync(hS.data(), dS, 8 * plen2, cudaMemcpyDeviceToHost, ctx->stream), "copy S");
-  if (!st) st = cuda_check(cudaMemcpyAsync(hT.data(), ctx->d_terms, 8 * plen2 * (2 + pd), cudaMemcpyDeviceToHost,
+  if (!st) st = cuda_check(cudaMemcpyAsync(hT.data(), ctx->d_terms, 8 * plen2 * (nfix + pd), cudaMemcpyDeviceToHost,
                                            ctx->stream), "copy terms");
   cudaFreeAsync(dS, ctx->stream);
   if (!st) st = cuda_check(cudaStreamSynchronize(ctx->stream), "write sync");
   if (st) return st;
   Writer w{root, {}};
   const std::vector<long long> dims = {2, (long long)plen};
-  // stored terms: 0 = NP, 1 = KE, 2 + j = V_j
+  // stored terms: 0 = NP, 1 = KE, 2 = MV (rel = 1), then V_j
   for (int k = 0; k < nk; ++k) {
     const std::string kn = name7(k + 1);
     if ((st = w.dataset("atomIntgGroup/atomOverlap/" + kn, dims, hS.data() + 2 * plen * k))) return st;
     if ((st = w.dataset("atomIntgGroup/atomKEOverlap/" + kn, dims, hT.data() + plen2 + 2 * plen * k))) return st;
+    if (ctx->rel &&
+        (st = w.dataset("atomIntgGroup/atomMVOverlap/" + kn, dims, hT.data() + 2 * plen2 + 2 * plen * k))) return st;
     if ((st = w.dataset("atomIntgGroup/atomNucOverlap/" + kn, dims, hT.data() + 2 * plen * k))) return st;
     for (int j = 0; j < pd; ++j)
       if ((st = w.dataset("atomIntgGroup/atomPotOverlap/" + kn + "/" + name7(j + 1), dims,
-                          hT.data() + (size_t)(2 + j) * plen2 + 2 * plen * k))) return st;
+                          hT.data() + (size_t)(nfix + j) * plen2 + 2 * plen * k))) return st;
   }
   return w.finish("setup-temp.hdf5");
 }

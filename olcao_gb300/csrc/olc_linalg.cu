@@ -478,22 +478,25 @@ int scf_prepare(olc_context* ctx, int precision, int form) {
                           nullptr, ctx->d_chol, nullptr))) return st;
   count_launch();
   hermitize_kernel<<<grid_for(nn * nk), 256, 0, ctx->stream>>>(ctx->d_chol, nv, nk);
+  const int nfix = 2 + ctx->rel;          // NP, KE (, MV) ahead of the V_j
   if (form == OLC_FORM_STORED) {
-    if (!ctx->d_terms && (st = dalloc(ctx, &ctx->d_terms, plen2 * (2 + pd)))) return st;
-    // term 0 = NP, 1 = KE, 2 + j = V_j (the order the reference sums them)
-    const int ops[2] = {OLC_OP_NUCLEAR, OLC_OP_KINETIC};
-    for (int t = 0; t < 2 + pd; ++t) {
-      const int op = t < 2 ? ops[t] : OLC_OP_ELECPOT;
-      if ((st = run_primitives(ctx, op, t < 2 ? 0 : t - 2, nullptr, OLC_PREC_FP64, false))) return st;
+    if (!ctx->d_terms && (st = dalloc(ctx, &ctx->d_terms, plen2 * (nfix + pd)))) return st;
+    // term 0 = NP, 1 = KE, 2 = MV when rel = 1, then V_j (the order the
+    // reference sums them, secularEqn.F90:128-150)
+    const int ops[3] = {OLC_OP_NUCLEAR, OLC_OP_KINETIC, OLC_OP_MASSVEL};
+    for (int t = 0; t < nfix + pd; ++t) {
+      const int op = t < nfix ? ops[t] : OLC_OP_ELECPOT;
+      if ((st = run_primitives(ctx, op, t < nfix ? 0 : t - nfix, nullptr, OLC_PREC_FP64, false))) return st;
       if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
       if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc,
                               ctx->d_scv, ctx->d_terms + (size_t)t * plen2, nullptr, nullptr))) return st;
     }
   } else {
     if (!ctx->d_h0 && (st = dalloc(ctx, &ctx->d_h0, 2 * nn * nk))) return st;
-    // H0 = KE + NP in one pass
+    // H0 = KE + NP (+ MV) in one pass
     if ((st = run_primitives(ctx, OLC_OP_KINETIC, 0, nullptr, OLC_PREC_FP64, false))) return st;
     if ((st = run_primitives(ctx, OLC_OP_NUCLEAR, 0, nullptr, OLC_PREC_FP64, true))) return st;
+    if (ctx->rel && (st = run_primitives(ctx, OLC_OP_MASSVEL, 0, nullptr, OLC_PREC_FP64, true))) return st;
     if ((st = run_contract_bloch(ctx, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc))) return st;
     if ((st = ortho_pack_ex(ctx, false, ctx->d_work_vv, ctx->d_work_cv, ctx->d_work_cc, ctx->d_scv,
                             nullptr, ctx->d_h0, nullptr))) return st;
@@ -638,8 +641,8 @@ int build_hamiltonian(olc_context* ctx, const double* coeffs, int precision, int
   // coefficients on the device; the reference adds a term whose multiplier
   // is exactly 0 unscaled (matrixSubs.F90:278-282)
   double* dco = nullptr;
-  const int off = ctx->prep_form == OLC_FORM_STORED ? 2 : 0;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dco, sizeof(double) * (pd + 2), ctx->stream), "malloc coeffs"))) return st;
+  const int off = ctx->prep_form == OLC_FORM_STORED ? 2 + ctx->rel : 0;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&dco, sizeof(double) * (pd + 3), ctx->stream), "malloc coeffs"))) return st;
   if (flags & OLC_ITER_COEFF_DEVICE) {
     cudaMemcpyAsync(dco + off, coeffs, sizeof(double) * pd, cudaMemcpyDeviceToDevice, ctx->stream);
   } else {
@@ -650,7 +653,7 @@ int build_hamiltonian(olc_context* ctx, const double* coeffs, int precision, int
   if (ctx->prep_form == OLC_FORM_STORED) {
     const size_t plen = (size_t)ctx->dims.packed_len;
     StageScope scope(ctx, OLC_STAGE_ASSEMBLE);
-    assemble_full_kernel<<<grid_for(plen * nk), 256, 0, ctx->stream>>>(ctx->d_terms, dco, pd + 2,
+    assemble_full_kernel<<<grid_for(plen * nk), 256, 0, ctx->stream>>>(ctx->d_terms, dco, pd + off,
                                                                         nv, nk, h);
     if ((st = cuda_check(cudaGetLastError(), "assemble_full_kernel"))) return st;
   } else {

@@ -6,6 +6,7 @@
 // angular class (L1, L2) so that every loop is unrolled:
 //   overlap      == overlap2CIntg   (gaussIntegrals.f90:26-4420)
 //   kinetic      == kinetic2CIntg   (gaussIntegrals.f90:4422-11622)
+//   mass velocity== massvel2CIntg   (gaussIntegrals.f90:39070-49402)
 //   elec 3-centre== electron3CIntg  (gaussIntegrals.f90:11624-16023)
 //   nuclear      == nuclear3CIntg   (gaussIntegrals.f90:16223-23039)
 // with the Boys function evaluated in the reference's formulation
@@ -181,6 +182,59 @@ __device__ __forceinline__ void add_kinetic(double a1, double a2, const double* 
   for (int a = 0; a < N1; ++a)
 #pragma unroll
     for (int b = 0; b < N2; ++b) cart[a * N2 + b] += w * T[a][b];
+}
+
+// Mass velocity: w (alpha^2 / 8) <a| nabla^4 |b> with alpha = fineStructure
+// x 1e-3 (constants.f90:47), the quantity massvel2CIntg returns
+// (gaussIntegrals.f90:39070-49402).  nabla^4 = sum_i d4_i + 2 sum_{i<j} d2_i d2_j
+// acts on b; per direction, on x^l exp(-a2 x^2),
+//   d2 -> l(l-1) x^(l-2) - 2 a2 (2l+1) x^l + 4 a2^2 x^(l+2)   (times the Gaussian)
+// and d4 is d2 applied twice, so every factor is a short combination of
+// 1-D overlaps with b's power raised by at most 4.
+constexpr double kFineStructure = 7.2973525693e-3;
+template <int LI, int LJ>
+__device__ __forceinline__ double lap1d(const double (&s)[LI + 1][LJ + 5], int i, int j, double a2) {
+  double v = -2.0 * a2 * (2 * j + 1) * s[i][j] + 4.0 * a2 * a2 * s[i][j + 2];
+  if (j >= 2) v += j * (j - 1) * s[i][j - 2];
+  return v;
+}
+template <int LI, int LJ>
+__device__ __forceinline__ double lap2d(const double (&s)[LI + 1][LJ + 5], int i, int j, double a2) {
+  double v = -2.0 * a2 * (2 * j + 1) * lap1d<LI, LJ>(s, i, j, a2) +
+             4.0 * a2 * a2 * lap1d<LI, LJ>(s, i, j + 2, a2);
+  if (j >= 2) v += j * (j - 1) * lap1d<LI, LJ>(s, i, j - 2, a2);
+  return v;
+}
+template <int L1, int L2>
+__device__ __forceinline__ void add_massvel(double a1, double a2, const double* A,
+                                            const double* B, double w, double* cart) {
+  constexpr int N1 = ncart(L1), N2 = ncart(L2);
+  const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
+  double s[3][L1 + 1][L2 + 5];
+  double d2 = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double P = (a1 * A[c] + a2 * B[c]) / z;
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    os1d<L1, L2 + 4>(P - A[c], P - B[c], inv2z, s[c]);
+  }
+  const double r = kPi / z;
+  const double pref = w * (kFineStructure * kFineStructure / 8.0) * r * sqrt(r) * exp(-xi * d2);
+#pragma unroll
+  for (int a = 0; a < N1; ++a)
+#pragma unroll
+    for (int b = 0; b < N2; ++b) {
+      double i0[3], i2[3], i4[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int ia = cexp(a, c), jb = cexp(b, c);
+        i0[c] = s[c][ia][jb];
+        i2[c] = lap1d<L1, L2>(s[c], ia, jb, a2);
+        i4[c] = lap2d<L1, L2>(s[c], ia, jb, a2);
+      }
+      cart[a * N2 + b] += pref * (i4[0] * i0[1] * i0[2] + i0[0] * i4[1] * i0[2] + i0[0] * i0[1] * i4[2] +
+                                  2.0 * (i2[0] * i2[1] * i0[2] + i2[0] * i0[1] * i2[2] + i0[0] * i2[1] * i2[2]));
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -131,6 +131,8 @@ int build_system(olc_context* ctx, const olc_system_t* s) {
     return fail(OLC_ERR_ARG, "olc_create: incomplete system description");
   if (!(s->basis_fn_thresh > 0.0 && s->basis_fn_thresh < 1.0))
     return fail(OLC_ERR_ARG, "olc_create: basis_fn_thresh must be in (0,1)");
+  if (s->rel != 0 && s->rel != 1) return fail(OLC_ERR_ARG, "olc_create: rel must be 0 or 1");
+  ctx->rel = s->rel;
   Lattice lat;
   for (int i = 0; i < 3; ++i)
     for (int c = 0; c < 3; ++c) lat.rv[i][c] = s->real_vectors[i * 3 + c];

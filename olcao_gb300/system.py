@@ -64,7 +64,8 @@ class SystemStruct(C.Structure):
                 ("pot_site_pos", C.POINTER(C.c_double)),
                 ("num_kpoints", C.c_int32),
                 ("kpoints_abc", C.POINTER(C.c_double)),
-                ("basis_fn_thresh", C.c_double)]
+                ("basis_fn_thresh", C.c_double),
+                ("rel", C.c_int32)]
 
 
 @dataclass
@@ -109,6 +110,7 @@ class System:
     pot_coeffs: np.ndarray             # [pot_dim]
     thresh: float = 1e-16
     seed: int = 0
+    rel: int = 0                       # 1: scalar relativistic (mass-velocity term)
     _keep: list = field(default_factory=list, repr=False)
 
     # ---- derived sizes -------------------------------------------------
@@ -181,6 +183,7 @@ class System:
         s.num_kpoints = self.num_kpoints
         s.kpoints_abc = arrs["kp"].ctypes.data_as(C.POINTER(C.c_double))
         s.basis_fn_thresh = self.thresh
+        s.rel = int(self.rel)
         self._keep[:] = [at, pt, arrs]
         return s
 

@@ -38,7 +38,10 @@ import numpy as np
 PI = 3.141592653589793  # src/constants.f90:36
 
 _SUBROUTINES = ("overlap2CIntg", "kinetic2CIntg", "electron3CIntg",
-                "nuclear3CIntg", "boys")
+                "nuclear3CIntg", "massvel2CIntg", "boys")
+# fineStructure of src/constants.f90:47 (in units of 1e-3), the only
+# module constant besides pi that the generated integrals read
+FINE_STRUCTURE = 7.2973525693
 _FUNCS = {"exp": "_exp", "sqrt": "_sqrt", "sum": "_sum", "erf": "_erf",
           "abs": "abs"}
 _VECTORS = {"p", "pa", "pb", "g", "ga", "gb", "gc", "pc_3c", "d", "d1", "d2",
@@ -68,7 +71,7 @@ def _erf(x):
 _TOKEN = re.compile(r"""
     (?P<num>(\d+\.\d*|\.\d+|\d+)([dDeE][-+]?\d+)?)
   | (?P<name>[A-Za-z_][A-Za-z_0-9]*)
-  | (?P<op>\*\*|[-+*/(),=])
+  | (?P<op>\*\*|[-+*/(),=:])
   | (?P<ws>\s+)
 """, re.VERBOSE)
 
@@ -129,7 +132,9 @@ def _translate(expr: str) -> str:
                 src = " ".join(_literal(v) if k == "num" else
                                (v.lower() if k == "name" else v)
                                for k, v in inner)
-                if val in _VECTORS:
+                if src.strip() == ":":
+                    out.append(val)            # whole-array section name(:)
+                elif val in _VECTORS:
                     out.append(f"{val}[({src})-1]")
                 else:
                     out.append(f"{val}[({src},)]")
@@ -253,17 +258,18 @@ class FortranIntegrals:
                     "kinetic2CIntg": "a1, a2, a, b, l1l2switch",
                     "electron3CIntg": "a1, a2, a3, a, b, c, l1l2switch",
                     "nuclear3CIntg": "a1, a2, a3, a, b, c, l1l2switch",
+                    "massvel2CIntg": "a1, a2, a, b, l1l2switch",
                     "boys": "t"}[name]
             if name == "boys":
                 pre = "    s = {}\n    f = {}\n"
                 post = "\n    return [f[(m,)] for m in range(1, 8)]"
             else:
-                pre = ("    pc = {}\n    pc_ol = {}\n    sh = {}\n"
+                pre = ("    pc = {}\n    pc_ol = {}\n    pc_ke = {}\n    sh = {}\n"
                        "    prefactorn = {}\n    f = {}\n")
                 post = "\n    return sh"
             code = f"def _{name}({args}):\n{pre}{body}{post}\n"
             ns = {"_exp": _exp, "_sqrt": _sqrt, "_sum": _sum, "_erf": _erf,
-                  "pi": PI, "np": np, "math": math}
+                  "pi": PI, "finestructure": FINE_STRUCTURE, "np": np, "math": math}
             exec(compile(code, f"<{name}>", "exec"), ns)
             self.__dict__["_fn_" + name] = ns["_" + name]
             if name == "boys":
@@ -296,6 +302,10 @@ class FortranIntegrals:
 
     def kinetic(self, a1, a2, A, B, switch):
         return self._run("kinetic2CIntg", float(a1), float(a2),
+                         np.asarray(A, float), np.asarray(B, float), int(switch))
+
+    def massvel(self, a1, a2, A, B, switch):
+        return self._run("massvel2CIntg", float(a1), float(a2),
                          np.asarray(A, float), np.asarray(B, float), int(switch))
 
     def electron3c(self, a1, a2, a3, A, B, C, switch):

@@ -77,7 +77,7 @@ const Harm kHarm[16] = {
 int lmax_of(int lmalpha) { return lmalpha == 1 ? 0 : lmalpha == 4 ? 1 : lmalpha == 9 ? 2 : 3; }
 
 // 1-D Obara-Saika overlap table s[i][j], i <= li, j <= lj (unit prefactor).
-void os_1d(double pa, double pb, double inv2z, int li, int lj, double s[6][6]) {
+void os_1d(double pa, double pb, double inv2z, int li, int lj, double s[8][8]) {
   s[0][0] = 1.0;
   for (int i = 0; i <= li; ++i) {
     if (i > 0) {
@@ -110,7 +110,7 @@ void prim_overlap(double a1, double a2, const double* A, const double* B,
                   int lma1, int lma2, double* sh) {
   const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
   const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
-  double d2 = 0, s[3][6][6];
+  double d2 = 0, s[3][8][8];
   for (int c = 0; c < 3; ++c) {
     double P = (a1 * A[c] + a2 * B[c]) / z;
     d2 += (A[c] - B[c]) * (A[c] - B[c]);
@@ -131,7 +131,7 @@ void prim_kinetic(double a1, double a2, const double* A, const double* B,
                   int lma1, int lma2, double* sh) {
   const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
   const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
-  double d2 = 0, s[3][6][6], PA[3], PB[3];
+  double d2 = 0, s[3][8][8], PA[3], PB[3];
   for (int c = 0; c < 3; ++c) {
     double P = (a1 * A[c] + a2 * B[c]) / z;
     PA[c] = P - A[c];
@@ -202,11 +202,51 @@ void prim_kinetic(double a1, double a2, const double* A, const double* B,
   }, sh);
 }
 
+// Mass velocity (massvel2CIntg, gaussIntegrals.f90:39070-49402): the value
+// (alpha^2 / 8) <a| nabla^4 |b>, alpha = fineStructure x 1e-3
+// (constants.f90:47).  nabla^4 = sum_i d4_i + 2 sum_{i<j} d2_i d2_j acting on
+// b; per direction d2 [x^l e^{-a2 x^2}] = (l(l-1) x^{l-2} - 2 a2 (2l+1) x^l
+// + 4 a2^2 x^{l+2}) e^{-a2 x^2} and d4 = d2 d2, so each factor is a short
+// sum of 1-D overlaps with b's power raised by at most four.
+void prim_massvel(double a1, double a2, const double* A, const double* B,
+                  int lma1, int lma2, double* sh) {
+  const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
+  const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
+  double d2 = 0, s[3][8][8];
+  for (int c = 0; c < 3; ++c) {
+    double P = (a1 * A[c] + a2 * B[c]) / z;
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    os_1d(P - A[c], P - B[c], inv2z, l1, l2 + 4, s[c]);
+  }
+  const double fs = 7.2973525693e-3;
+  const double pref = fs * fs / 8.0 * std::pow(kPi / z, 1.5) * std::exp(-xi * d2);
+  auto lap = [&](int c, int i, int j) {          // <i| d2 |j>
+    double v = -2.0 * a2 * (2 * j + 1) * s[c][i][j] + 4.0 * a2 * a2 * s[c][i][j + 2];
+    if (j >= 2) v += j * (j - 1) * s[c][i][j - 2];
+    return v;
+  };
+  auto lap2 = [&](int c, int i, int j) {         // <i| d2 d2 |j>
+    double v = -2.0 * a2 * (2 * j + 1) * lap(c, i, j) + 4.0 * a2 * a2 * lap(c, i, j + 2);
+    if (j >= 2) v += j * (j - 1) * lap(c, i, j - 2);
+    return v;
+  };
+  cart_to_sh(lma1, lma2, [&](const int* ea, const int* eb) {
+    double i0[3], i2[3], i4[3];
+    for (int c = 0; c < 3; ++c) {
+      i0[c] = s[c][ea[c]][eb[c]];
+      i2[c] = lap(c, ea[c], eb[c]);
+      i4[c] = lap2(c, ea[c], eb[c]);
+    }
+    return pref * (i4[0] * i0[1] * i0[2] + i0[0] * i4[1] * i0[2] + i0[0] * i0[1] * i4[2] +
+                   2.0 * (i2[0] * i2[1] * i0[2] + i2[0] * i0[1] * i2[2] + i0[0] * i2[1] * i2[2]));
+  }, sh);
+}
+
 void prim_elec3c(double a1, double a2, double a3, const double* A, const double* B,
                  const double* Cc, int lma1, int lma2, double* sh) {
   const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
   const double z = a1 + a2, z3 = z + a3, inv2z3 = 1.0 / (2.0 * z3), xi = a1 * a2 / z;
-  double d2 = 0, pc2 = 0, s[3][6][6];
+  double d2 = 0, pc2 = 0, s[3][8][8];
   for (int c = 0; c < 3; ++c) {
     double P = (a1 * A[c] + a2 * B[c]) / z;
     double G = (a1 * A[c] + a2 * B[c] + a3 * Cc[c]) / z3;
@@ -715,6 +755,7 @@ struct Oracle {
               bool contrib = true;
               if (op == OLC_OP_OVERLAP) prim_overlap(al1, al2, A, Bs, lma1, lma2, sh);
               else if (op == OLC_OP_KINETIC) prim_kinetic(al1, al2, A, Bs, lma1, lma2, sh);
+              else if (op == OLC_OP_MASSVEL) prim_massvel(al1, al2, A, Bs, lma1, lma2, sh);
               else contrib = third_centre(op, ai[0], ai[1], e1, e2, lma1, lma2, sep, A, Bs,
                                           al1, al2, potType, potAlpha, sh);
               if (contrib) {
@@ -723,7 +764,9 @@ struct Oracle {
                   if (lm2 > lma2) continue;   // basis(alpha2, m) == 0 there
                   double c2 = t2.basis[ai[1]][m];
                   double* px = &pairX[(size_t)(m * OLC_MAX_ALPHAS + ai[0]) * 16];
-                  for (int a = 0; a < lma1; ++a) px[a] += sh[(lm2 - 1) * 16 + a] * c2;
+                  // gaussOverlapMV subtracts its primitive (integrals.F90:1228-1236)
+                  const double c2s = op == OLC_OP_MASSVEL ? -c2 : c2;
+                  for (int a = 0; a < lma1; ++a) px[a] += sh[(lm2 - 1) * 16 + a] * c2s;
                 }
                 maxA1 = std::max(maxA1, ai[0] + 1);
               }
@@ -912,7 +955,8 @@ void orc_ortho_pack(void* h, int is_overlap, double* vv, const double* cv, const
                 reinterpret_cast<const cplx*>(cc), reinterpret_cast<const cplx*>(scv), packed);
 }
 
-// Primitive evaluation: kind 1 overlap, 2 kinetic, 3 nuclear, 4 electron3C.
+// Primitive evaluation: kind 1 overlap, 2 kinetic, 3 nuclear, 4 electron3C,
+// 5 mass velocity.
 // in = (a1,a2,a3,A[3],B[3],C[3]); out = sh(16,16) column-major.
 void orc_primitive(int kind, const double* in, const int32_t* lmalpha, double* out) {
   for (int q = 0; q < 256; ++q) out[q] = 0.0;
@@ -922,6 +966,7 @@ void orc_primitive(int kind, const double* in, const int32_t* lmalpha, double* o
     case 2: prim_kinetic(in[0], in[1], A, B, lmalpha[0], lmalpha[1], out); break;
     case 3: prim_nuclear(in[0], in[1], in[2], A, B, Cc, lmalpha[0], lmalpha[1], out); break;
     case 4: prim_elec3c(in[0], in[1], in[2], A, B, Cc, lmalpha[0], lmalpha[1], out); break;
+    case 5: prim_massvel(in[0], in[1], A, B, lmalpha[0], lmalpha[1], out); break;
   }
 }
 

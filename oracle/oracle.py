@@ -20,7 +20,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB: Optional[C.CDLL] = None
 
-OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT = 1, 2, 3, 4
+OP_OVERLAP, OP_KINETIC, OP_NUCLEAR, OP_ELECPOT, OP_MASSVEL = 1, 2, 3, 4, 5
 
 
 def build() -> str:
@@ -122,7 +122,10 @@ class Oracle:
         OLCAOsetup writes them (integrals.F90 ortho + pack)."""
         vvS, cvS, ccS = self.operator(OP_OVERLAP)
         out = {"S": self.ortho_pack(True, vvS, cvS, ccS, cvS)}
-        for name, op in (("KE", OP_KINETIC), ("NP", OP_NUCLEAR)):
+        ops = (("KE", OP_KINETIC), ("NP", OP_NUCLEAR))
+        if getattr(self.system, "rel", 0):
+            ops += (("MV", OP_MASSVEL),)      # gaussOverlapMV, OLCAO_Setup.f90:142-144
+        for name, op in ops:
             vv, cv, cc = self.operator(op)
             out[name] = self.ortho_pack(False, vv, cv, cc, cvS)
         terms = range(self.pot_dim) if terms is None else terms
@@ -134,9 +137,12 @@ class Oracle:
 
 def assemble(packed: Dict[str, np.ndarray], coeffs: np.ndarray) -> np.ndarray:
     """secularEqn.F90:128-150 with readPackedMatrixAccum's rule that a zero
-    multiplier adds the term unscaled (matrixSubs.F90:278-282)."""
+    multiplier adds the term unscaled (matrixSubs.F90:278-282); the mass
+    velocity joins when present (rel = 1, :137-143)."""
     h = packed["NP"].copy()
     h = h + packed["KE"]
+    if "MV" in packed:
+        h = h + packed["MV"]
     for j, c in enumerate(coeffs):
         v = packed[f"V{j}"]
         h = h + v if c == 0.0 else h + v * c
@@ -208,15 +214,16 @@ def make_valence_rho(packed: Dict[str, np.ndarray], pot_dim: int, occupation: np
     for spin 2 turned into (up + down, up - down) (:307-313), and traced with
     S, NP, KE and every V_j (:321-395).
 
-    Returns (traces [spin, 3 + pot_dim] = charge, nuclear, kinetic, potRho,
-    electron energy [spin], packed rho [spin, nk, plen, 2])."""
+    Returns (traces [spin, 3 + rel + pot_dim] = charge, nuclear, kinetic,
+    mass velocity (when packed holds "MV"), potRho; electron energy [spin];
+    packed rho [spin, nk, plen, 2])."""
     spin, nk, ns = occupation.shape
     n = vectors.shape[-1]
     rows, cols = packed_index(n)
-    traces = np.zeros((spin, 3 + pot_dim))
+    names = ["S", "NP", "KE"] + (["MV"] if "MV" in packed else []) + [f"V{j}" for j in range(pot_dim)]
+    traces = np.zeros((spin, len(names)))
     energy = np.zeros(spin)
     rho_packed = np.zeros((spin, nk, rows.size, 2))
-    names = ["S", "NP", "KE"] + [f"V{j}" for j in range(pot_dim)]
     for k in range(nk):
         keep = [j for j in range(ns) if np.abs(occupation[:, k, j]).sum() >= SMALL_THRESH]
         for j in keep:
@@ -234,3 +241,59 @@ def make_valence_rho(packed: Dict[str, np.ndarray], pot_dim: int, occupation: np
             for t, name in enumerate(names):
                 traces[s, t] += matrix_element_mult(packed[name][k], pk[s])
     return traces, energy, rho_packed
+
+
+def massvel_scale(a1: float, a2: float, A, B, l1: int, l2: int) -> float:
+    """Rounding scale of a mass-velocity block: the largest Cartesian element
+    of (alpha^2/8) <a|nabla^4|b> with every term of its expansion in 1-D
+    overlaps (the one prim_massvel evaluates) taken in absolute value.  Two
+    correct FP64 evaluations of the block agree to a small multiple of
+    2^-52 times this; with very unequal exponents the terms cancel to many
+    digits, so the block itself can be far smaller than the scale."""
+    A = np.asarray(A, float)
+    B = np.asarray(B, float)
+    z = a1 + a2
+    inv2z = 1.0 / (2.0 * z)
+    xi = a1 * a2 / z
+    P = (a1 * A + a2 * B) / z
+    pref = (np.pi / z) ** 1.5 * np.exp(-xi * np.sum((A - B) ** 2))
+    tabs = []
+    for c in range(3):
+        pa, pb = abs(P[c] - A[c]), abs(P[c] - B[c])
+        s = np.zeros((l1 + 1, l2 + 5))
+        s[0, 0] = 1.0
+        for i in range(l1 + 1):
+            if i > 0:
+                s[i, 0] = pa * s[i - 1, 0] + ((i - 1) * inv2z * s[i - 2, 0] if i > 1 else 0.0)
+            for j in range(1, l2 + 5):
+                v = pb * s[i, j - 1]
+                if i > 0:
+                    v += i * inv2z * s[i - 1, j - 1]
+                if j > 1:
+                    v += (j - 1) * inv2z * s[i, j - 2]
+                s[i, j] = v
+        tabs.append(s)
+
+    def d2(j):
+        out = [(j, 2 * a2 * (2 * j + 1)), (j + 2, 4 * a2 * a2)]
+        return out + ([(j - 2, j * (j - 1))] if j >= 2 else [])
+
+    def lap(s, i, j):
+        return sum(w * s[i, m] for m, w in d2(j))
+
+    def lap2(s, i, j):
+        return sum(w * lap(s, i, m) for m, w in d2(j))
+
+    def cart(l):
+        return [(x, y, n - x - y) for n in range(l + 1) for x in range(n, -1, -1) for y in range(n - x, -1, -1)]
+
+    best = 0.0
+    for ea in cart(l1):
+        for eb in cart(l2):
+            i0 = [tabs[c][ea[c], eb[c]] for c in range(3)]
+            i2 = [lap(tabs[c], ea[c], eb[c]) for c in range(3)]
+            i4 = [lap2(tabs[c], ea[c], eb[c]) for c in range(3)]
+            v = (i4[0] * i0[1] * i0[2] + i0[0] * i4[1] * i0[2] + i0[0] * i0[1] * i4[2]
+                 + 2 * (i2[0] * i2[1] * i0[2] + i2[0] * i0[1] * i2[2] + i0[0] * i2[1] * i2[2]))
+            best = max(best, v)
+    return 3.0 * best * pref * (7.2973525693e-3) ** 2 / 8.0

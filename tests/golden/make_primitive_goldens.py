@@ -7,11 +7,15 @@ generated Fortran statements verbatim in binary64):
     python tests/golden/make_primitive_goldens.py [path/to/gaussIntegrals.f90]
 
 The fixture holds, for overlap2CIntg (kind 1), kinetic2CIntg (2),
-nuclear3CIntg (3) and electron3CIntg (4), seeded inputs for every
-(lmAlpha1, lmAlpha2) block the reference generates (s/p/d/f except f-f, which
-gaussIntegrals.f90 has no block for) plus edge cases (coincident centres,
-Boys argument at and around the reference's 0.1 series/closed-form switch,
-extreme exponents, large separations), and the Boys values F_0..F_6 on a grid.
+nuclear3CIntg (3), electron3CIntg (4) and massvel2CIntg (5), seeded inputs
+for every (lmAlpha1, lmAlpha2) block the reference generates (s/p/d/f; f-f
+only for the mass velocity, the one routine with an f-f block) plus edge
+cases (coincident centres, Boys argument at and around the reference's 0.1
+series/closed-form switch, extreme exponents, large separations), and the
+Boys values F_0..F_6 on a grid.  For kind 5 it also stores the rounding
+scale of each block (oracle.massvel_scale): with very unequal exponents the
+nabla^4 expansion cancels to many digits and both the reference's and any
+other FP64 evaluation are only accurate relative to that scale.
 """
 
 import os
@@ -22,6 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
 import fexpr_eval as fe  # noqa: E402
+import oracle as orc  # noqa: E402
 
 LMS = (1, 4, 9, 16)
 
@@ -30,7 +35,7 @@ def main(path=None):
     path = path or fe.default_path()
     F = fe.FortranIntegrals(path)
     rng = np.random.default_rng(20261203)
-    params, lmal, kinds, outs = [], [], [], []
+    params, lmal, kinds, outs, scales = [], [], [], [], []
 
     def add(kind, a1, a2, a3, A, B, Cc, l1, l2):
         sw = fe.l1l2switch(l1, l2)
@@ -40,8 +45,12 @@ def main(path=None):
             sh = F.kinetic(a1, a2, A, B, sw)
         elif kind == 3:
             sh = F.nuclear3c(a1, a2, a3, A, B, Cc, sw)
-        else:
+        elif kind == 4:
             sh = F.electron3c(a1, a2, a3, A, B, Cc, sw)
+        else:
+            sh = F.massvel(a1, a2, A, B, sw)
+        lof = {1: 0, 4: 1, 9: 2, 16: 3}
+        scales.append(orc.massvel_scale(a1, a2, A, B, lof[l1], lof[l2]) if kind == 5 else np.nan)
         block = np.full((16, 16), np.nan)
         block[:l1, :l2] = sh[:l1, :l2]
         params.append([a1, a2, a3, *A, *B, *Cc])
@@ -49,10 +58,10 @@ def main(path=None):
         kinds.append(kind)
         outs.append(block)
 
-    for kind in (1, 2, 3, 4):
+    for kind in (1, 2, 3, 4, 5):
         for l1 in LMS:
             for l2 in LMS:
-                if l1 == 16 and l2 == 16:
+                if l1 == 16 and l2 == 16 and kind != 5:
                     continue
                 for t in range(8):
                     a1, a2, a3 = np.exp(rng.uniform(np.log(0.12), np.log(80.0), 3))
@@ -83,6 +92,7 @@ def main(path=None):
     out = os.path.join(HERE, "primitives.npz")
     np.savez_compressed(out, params=np.array(params), lmalpha=np.array(lmal, np.int32),
                         kind=np.array(kinds, np.int32), sh=np.array(outs),
+                        scale=np.array(scales),
                         boys_T=grid, boys_F=boys,
                         source=np.array(os.path.relpath(path, os.path.dirname(path) + "/../..")))
     print(f"wrote {out}: {len(kinds)} primitive blocks, {len(grid)} Boys points")

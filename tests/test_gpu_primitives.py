@@ -17,6 +17,23 @@ def _block_err(ref, got, l1, l2):
 
 
 @pytest.mark.gpu
+def test_device_massvel_matches_reference(gpu_lib, golden):
+    """massvel2CIntg: agreement to rounding of the nabla^4 expansion's
+    scale (both sides cancel the same large terms at unequal exponents)."""
+    from olcao_gb300 import api
+    sel = (golden["kind"] == 5) & (golden["lmalpha"].max(axis=1) <= 9)
+    params = golden["params"][sel]
+    lm = golden["lmalpha"][sel]
+    ref = golden["sh"][sel]
+    scale = golden["scale"][sel]
+    got = api.primitive_batch(5, params, lm)
+    for i in range(len(params)):
+        l1, l2 = lm[i]
+        diff = np.abs(got[i][:l1, :l2] - ref[i][:l1, :l2]).max()
+        assert diff <= 16 * 2.0 ** -52 * scale[i], f"item {i} lm {lm[i]}: {diff:.2e} of {scale[i]:.2e}"
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("kind", [1, 2, 3, 4])
 def test_device_primitives_match_reference(gpu_lib, golden, kind):
     from olcao_gb300 import api
