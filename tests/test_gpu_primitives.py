@@ -19,7 +19,10 @@ def _block_err(ref, got, l1, l2):
 @pytest.mark.gpu
 def test_device_massvel_matches_reference(gpu_lib, golden):
     """massvel2CIntg: agreement to rounding of the nabla^4 expansion's
-    scale (both sides cancel the same large terms at unequal exponents)."""
+    scale (both sides cancel the same large terms at unequal exponents),
+    plus the 1e-12 relative bar of the other kinds, which covers the
+    conditioning of exp(-xi |AB|^2) at large separations (an argument near
+    140 carries ~3e-14 relative error from its own last bit)."""
     from olcao_gb300 import api
     sel = (golden["kind"] == 5) & (golden["lmalpha"].max(axis=1) <= 9)
     params = golden["params"][sel]
@@ -30,7 +33,8 @@ def test_device_massvel_matches_reference(gpu_lib, golden):
     for i in range(len(params)):
         l1, l2 = lm[i]
         diff = np.abs(got[i][:l1, :l2] - ref[i][:l1, :l2]).max()
-        assert diff <= 16 * 2.0 ** -52 * scale[i], f"item {i} lm {lm[i]}: {diff:.2e} of {scale[i]:.2e}"
+        tol = 16 * 2.0 ** -52 * scale[i] + 1e-12 * np.abs(ref[i][:l1, :l2]).max()
+        assert diff <= tol, f"item {i} lm {lm[i]}: {diff:.2e} of {scale[i]:.2e}"
 
 
 @pytest.mark.gpu
