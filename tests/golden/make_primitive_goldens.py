@@ -8,11 +8,12 @@ generated Fortran statements verbatim in binary64):
 
 The fixture holds, for overlap2CIntg (kind 1), kinetic2CIntg (2),
 nuclear3CIntg (3), electron3CIntg (4) and massvel2CIntg (5), seeded inputs
-for every (lmAlpha1, lmAlpha2) block the reference generates (s/p/d/f; f-f
-only for the mass velocity, the one routine with an f-f block) plus edge
-cases (coincident centres, Boys argument at and around the reference's 0.1
+for every (lmAlpha1, lmAlpha2) block the reference generates (s/p/d/f, the
+f-f block being each routine's final `else`) plus edge cases (coincident
+centres, Boys argument at and around the reference's 0.1
 series/closed-form switch, extreme exponents, large separations), and the
-Boys values F_0..F_6 on a grid.  For kind 5 it also stores the rounding
+Boys values F_0..F_6 on a grid.  The f-f blocks of kinds 1-4 come last
+(drawn after everything else, so the earlier entries keep their inputs).  For kind 5 it also stores the rounding
 scale of each block (oracle.massvel_scale): with very unequal exponents the
 nabla^4 expansion cancels to many digits and both the reference's and any
 other FP64 evaluation are only accurate relative to that scale.
@@ -86,6 +87,16 @@ def main(path=None):
                     if t == 4:
                         B = A + rng.standard_normal(3) * 4.0
                     add(kind, a1, a2, a3, A, B, Cc, l1, l2)
+    # f-f blocks of kinds 1-4 (`else ! switch 136` of each routine)
+    for kind in (1, 2, 3, 4):
+        for t in range(6):
+            a1, a2, a3 = np.exp(rng.uniform(np.log(0.12), np.log(80.0), 3))
+            A, B, Cc = rng.uniform(-2.0, 2.0, (3, 3))
+            if t == 0:
+                B = A.copy()
+            if t == 1:
+                Cc = A.copy()
+            add(kind, a1, a2, a3, A, B, Cc, 16, 16)
     grid = np.concatenate([[0.0, 1e-12, 1e-6, 0.05, 0.0999999, 0.1, 0.10000001,
                             0.1000001, 0.2], np.geomspace(0.3, 80.0, 40)])
     boys = np.array([F.boys(T) for T in grid])
