@@ -36,6 +36,8 @@
  *                              potential-dependent integrals recomputed
  *                              (src/olcao/secularEqn.F90:33-287,
  *                               src/uolcao/integrals.F90:2860-3605 fused form)
+ *   olc_populate_states        populateStates: occupations and Fermi level
+ *                              (src/olcao/populate.F90:132-578)
  *   olc_make_valence_rho       makeValenceRho: density and operator traces
  *                              (src/olcao/valeCharge.F90:34-420)
  */
@@ -323,6 +325,24 @@ int olc_make_valence_rho(olc_context_t* ctx, int num_states, int spin,
                          const double* occupation, const double* eigenvalues,
                          const double* vectors, double* traces,
                          double* electron_energy, double* rho_packed);
+
+/* populateStates (src/olcao/populate.F90:132-578): occupations of the
+ * eigenstates, host arrays only (no context).  eigenvalues[num_states, nk,
+ * spin] (Hartree), kpoint_weights[nk] (kPointWeight; each state holds
+ * weight / spin electrons).  The states are sorted as the reference sorts
+ * them (its merge, ties included), filled up to num_electrons, and the
+ * charge of the highest occupied level is spread over the states within
+ * 1e-8 Ha of it; with thermal_sigma != 0 (Hartree) the Fermi energy is then
+ * found by the reference's bisection with the smeared step function cut at
+ * +-max_thermal_range, starting fermi_search_limit (Hartree) outside the
+ * highest occupied and the next state.  Writes occupation[num_states, nk,
+ * spin] (structuredElectronPopulation, the input of olc_make_valence_rho)
+ * and, if not NULL, the highest occupied (Fermi) energy.  XANES core holes
+ * are not handled.  OLC_ERR_ARG when the states cannot hold num_electrons. */
+int olc_populate_states(int num_states, int num_kpoints, int spin, const double* eigenvalues,
+                        const double* kpoint_weights, double num_electrons, double thermal_sigma,
+                        double fermi_search_limit, double max_thermal_range,
+                        double* occupation, double* occupied_energy);
 
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the

@@ -17,6 +17,7 @@ this module                reference (src/olcao/...)
 ``solve_zhegv``            solveZHEGV         interfaces.F90:73-120
 ``scf_iteration``          secularEqnAllKP with the potential-dependent
                            integrals recomputed (fused form)
+``populate_states``        populateStates     populate.F90:132-578
 ``make_valence_rho``       makeValenceRho     valeCharge.F90:34-420
 =========================  ==================================================
 
@@ -48,7 +49,7 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
            "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
            "olc_split_zgemm", "olc_write_setup_integrals", "olc_write_eigen",
-           "olc_make_valence_rho")
+           "olc_make_valence_rho", "olc_populate_states")
 STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve", "refine",
           "density")
 
@@ -100,6 +101,8 @@ def lib() -> C.CDLL:
         L.olc_write_setup_integrals.argtypes = [vp, C.c_char_p]
         L.olc_write_eigen.argtypes = [C.c_char_p, i32, i32, i32, i32, dp, dp]
         L.olc_make_valence_rho.argtypes = [vp, i32, i32, dp, dp, dp, dp, dp, dp]
+        d = C.c_double
+        L.olc_populate_states.argtypes = [i32, i32, i32, dp, dp, d, d, d, d, dp, dp]
         L.olc_launch_count.restype = C.c_int64
         L.olc_launch_count.argtypes = []
         _LIB = L
@@ -157,6 +160,28 @@ def write_eigen(root: str, eigenvalues: np.ndarray, vectors: Optional[np.ndarray
         nv = vc.shape[2]
         vp = vc.ctypes.data
     _check(lib().olc_write_eigen(root.encode(), nk, spin, ns, nv, ev.ctypes.data, vp))
+
+
+def populate_states(eigenvalues, kpoint_weights, num_electrons: float,
+                    thermal_sigma: float = 0.0, fermi_search_limit: float = 0.5,
+                    max_thermal_range: float = 11.5):
+    """populateStates (populate.F90:132-578) on host arrays: eigenvalues
+    [spin, nk, num_states] or [nk, num_states] (Hartree), kpoint_weights [nk].
+    Returns (occupation of the same shape as eigenvalues, occupied energy)."""
+    ev = np.ascontiguousarray(eigenvalues, np.float64)
+    squeeze = ev.ndim == 2
+    if squeeze:
+        ev = ev[None]
+    spin, nk, ns = ev.shape
+    kw = np.ascontiguousarray(kpoint_weights, np.float64)
+    if kw.shape != (nk,):
+        raise ValueError(f"kpoint_weights has shape {kw.shape}, expected ({nk},)")
+    occ = np.zeros_like(ev)
+    ef = C.c_double()
+    _check(lib().olc_populate_states(ns, nk, spin, ev.ctypes.data, kw.ctypes.data, float(num_electrons),
+                                     float(thermal_sigma), float(fermi_search_limit),
+                                     float(max_thermal_range), occ.ctypes.data, C.addressof(ef)))
+    return (occ[0] if squeeze else occ), float(ef.value)
 
 
 def read_dataset(root: str, path: str) -> np.ndarray:

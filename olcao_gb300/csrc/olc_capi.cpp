@@ -330,6 +330,18 @@ int olc_write_eigen(const char* root, int num_kpoints, int spin, int num_states,
   return write_eigen(root, num_kpoints, spin, num_states, vale_dim, eigenvalues, vectors);
 }
 
+int olc_populate_states(int num_states, int num_kpoints, int spin, const double* eigenvalues,
+                        const double* kpoint_weights, double num_electrons, double thermal_sigma,
+                        double fermi_search_limit, double max_thermal_range, double* occupation,
+                        double* occupied_energy) {
+  if (num_states < 1 || num_kpoints < 1 || (spin != 1 && spin != 2) || !eigenvalues || !kpoint_weights ||
+      !occupation || !(num_electrons >= 0.0) || !(thermal_sigma >= 0.0) ||
+      (thermal_sigma > 0.0 && !(max_thermal_range > 0.0)))
+    return fail(OLC_ERR_ARG, "olc_populate_states: bad argument");
+  return populate_states(num_states, num_kpoints, spin, eigenvalues, kpoint_weights, num_electrons,
+                         thermal_sigma, fermi_search_limit, max_thermal_range, occupation, occupied_energy);
+}
+
 int olc_make_valence_rho(olc_context_t* ctx, int num_states, int spin, const double* occupation,
                          const double* eigenvalues, const double* vectors, double* traces,
                          double* electron_energy, double* rho_packed) {

@@ -281,6 +281,11 @@ void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
 // status of a queued mixed solve (olc_mixed.cu)
 int mixed_check_info(olc_context* ctx);
 
+// occupations (olc_populate.cpp, host)
+int populate_states(int num_states, int nk, int spin, const double* eig, const double* kweight,
+                    double num_electrons, double thermal_sigma, double fermi_search_limit,
+                    double max_thermal_range, double* occupation, double* occupied_energy);
+
 // valence density and its traces (olc_density.cu)
 int make_valence_rho(olc_context* ctx, int num_states, int spin, const double* occupation,
                      const double* eigenvalues, const double* vectors, double* traces,

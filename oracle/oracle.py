@@ -11,6 +11,7 @@ src/olcao/interfaces.F90:105 calls) on the unpacked H(k), S(k).
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 from typing import Dict, Optional, Sequence
@@ -297,3 +298,114 @@ def massvel_scale(a1: float, a2: float, A, B, l1: int, l2: int) -> float:
                  + 2 * (i2[0] * i2[1] * i0[2] + i2[0] * i0[1] * i2[2] + i0[0] * i2[1] * i2[2]))
             best = max(best, v)
     return 3.0 * best * pref * (7.2973525693e-3) ** 2 / 8.0
+
+
+# ---- occupations (the step before the valence density) ----------------------
+def merge_sort(values):
+    """The reference's bottom-up merge of adjacent runs (sortSubs.f90:18-175),
+    ties taken from the second run first.  Returns (sorted, order)."""
+    n = len(values)
+    a, oa = list(values), list(range(n))
+    b, ob = [0.0] * n, [0] * n
+    borders = list(range(n + 1))
+    nseg = n
+    src_a = True
+    while nseg > 1:
+        fd, fo, td, to = (a, oa, b, ob) if src_a else (b, ob, a, oa)
+        tp = 0
+        for i in range(nseg // 2):
+            p1, p2 = borders[2 * i], borders[2 * i + 1]
+            e1, e2 = borders[2 * i + 1], borders[2 * i + 2]
+            while tp < e2:
+                if p1 < e1 and (p2 >= e2 or fd[p1] < fd[p2]):
+                    td[tp], to[tp] = fd[p1], fo[p1]
+                    p1 += 1
+                else:
+                    td[tp], to[tp] = fd[p2], fo[p2]
+                    p2 += 1
+                tp += 1
+            borders[i + 1] = e2
+        if nseg % 2:
+            for q in range(tp, borders[nseg]):
+                td[q], to[q] = fd[q], fo[q]
+            borders[nseg // 2 + 1] = borders[nseg]
+        src_a = not src_a
+        nseg = nseg // 2 + nseg % 2
+    return (a, oa) if src_a else (b, ob)
+
+
+def populate_states(eigenvalues: np.ndarray, kpoint_weights: np.ndarray, num_electrons: float,
+                    thermal_sigma: float = 0.0, fermi_search_limit: float = 0.5,
+                    max_thermal_range: float = 11.5):
+    """populateStates (src/olcao/populate.F90:132-578): populateStandard,
+    then populateSmearing when thermal_sigma != 0.  eigenvalues [spin, nk,
+    num_states]; returns (occupation of that shape, occupied energy)."""
+    spin, nk, ns = eigenvalues.shape
+    vals, kpt = [], []
+    for k in range(nk):                   # k-point, spin, state (:224-232)
+        for s in range(spin):
+            for j in range(ns):
+                vals.append(float(eigenvalues[s, k, j]))
+                kpt.append(k)
+    srt, order = merge_sort(vals)
+    n = len(vals)
+
+    def w(i):
+        return kpoint_weights[kpt[order[i]]] / spin
+
+    pop = [0.0] * n
+    placed = 0.0
+    occ = None
+    for i in range(n):                    # :292-331
+        pop[order[i]] = w(i)
+        placed += pop[order[i]]
+        if placed > num_electrons:
+            pop[order[i]] = w(i) + num_electrons - placed
+            placed = num_electrons
+        if abs(num_electrons - placed) < SMALL_THRESH:
+            occ = i
+            break
+    if occ is None:
+        raise ValueError("the states hold fewer electrons than num_electrons")
+    e_occ = srt[occ]
+    lo = hi = occ                          # degenerate top level (:344-399)
+    charge, possible = pop[order[occ]], w(occ)
+    while hi + 1 < n and abs(e_occ - srt[hi + 1]) <= SMALL_THRESH:
+        hi += 1
+        possible += w(hi)
+    while lo > 0 and abs(e_occ - srt[lo - 1]) <= SMALL_THRESH:
+        lo -= 1
+        possible += w(lo)
+        charge += w(lo)
+    for i in range(lo, hi + 1):
+        pop[order[i]] = charge / possible * w(i)
+    occ = hi
+    e_occ = srt[occ]
+    if thermal_sigma != 0.0:               # :484-576
+        emin = srt[occ] - fermi_search_limit
+        emax = srt[min(occ + 1, n - 1)] + fermi_search_limit
+        for _ in range(500):
+            e_occ = 0.5 * (emin + emax)
+            total = 0.0
+            pop = [0.0] * n
+            for i in range(n):
+                x = (srt[i] - e_occ) / thermal_sigma
+                f = 0.0 if x > max_thermal_range else 1.0 if x < -max_thermal_range else 1.0 / (1.0 + math.exp(x))
+                if f == 0.0:
+                    break
+                pop[order[i]] = w(i) * f
+                total += pop[order[i]]
+            if abs(total - num_electrons) < SMALL_THRESH:
+                break
+            if total < num_electrons:
+                emin = e_occ
+            else:
+                emax = e_occ
+    out = np.zeros_like(eigenvalues, dtype=np.float64)
+    q = 0
+    for k in range(nk):
+        for s in range(spin):
+            for j in range(ns):
+                out[s, k, j] = pop[q]
+                q += 1
+    return out, e_occ
