@@ -11,15 +11,23 @@
 //   basis                     src/olcao/basis.f90:55-243
 //   screening tables          src/olcao/gaussRelations.f90:64-278
 //   integral drivers          src/olcao/integrals.F90:81-486 (OL), 490-900 (KE),
-//                             1324-1715 (NP), 1719-2122 (EP), 2275-2439
-//                             (nuclearPE), 2442-2598 (electronicPE)
+//                             904-1320 (MV), 1324-1715 (NP), 1719-2122 (EP),
+//                             2275-2439 (nuclearPE), 2442-2598 (electronicPE)
 //   pair scatter / phases     src/olcao/intgSaving.F90:56-550
 //   orthogonalisation, pack   src/olcao/intgOrtho.F90:23-187,
 //                             src/olcao/integrals.F90:2601-2853
 // Its Gaussian primitives are an independent Obara-Saika implementation
 // (Obara & Saika, J. Chem. Phys. 84, 3963 (1986)) checked against the
 // reference's own generated code (gaussIntegrals.f90) through the golden
-// vectors in tests/golden/.
+// vectors in tests/golden/, and against direct quadrature.
+//
+// Parity pinning: the primitives are pinned (the goldens are the reference's
+// own statements evaluated in binary64).  The driver level -- screening,
+// contraction, Bloch phases, scatter, orthogonalisation, packing, assembly --
+// is parity unpinned: the reference holds no fixtures for it and cannot be
+// built here (no Fortran compiler, no HDF5, no LAPACK development files), so
+// this restatement rests on its own reading of the reference plus brute-force
+// image sums, Hermiticity and the reference's printed identities.
 //
 // Notes on deliberate restatement choices (results identical up to rounding):
 // * findLatticeVector: the reference rounds each fractional coordinate and then

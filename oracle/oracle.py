@@ -5,7 +5,15 @@ cpu_baseline leg of bench.py as the checker, never by the product.
 
 Besides the compiled restatement of the reference loops this module holds the
 eigen-solve leg of the oracle: scipy's LAPACK ``zhegv`` (the routine
-src/olcao/interfaces.F90:105 calls) on the unpacked H(k), S(k).
+src/olcao/interfaces.F90:105 calls) on the unpacked H(k), S(k), and numpy
+restatements of the steps after the solve: populateStates
+(src/olcao/populate.F90:132-578, with the merge sort of sortSubs.f90:18-175)
+and makeValenceRho (src/olcao/valeCharge.F90:172-395).
+
+Parity pinning: primitives pinned by the reference's own generated code
+(tests/golden); everything above them -- drivers, eigen-solve call,
+occupations, density traces -- parity unpinned (no reference fixtures for
+this path, reference not buildable here).
 """
 
 from __future__ import annotations
