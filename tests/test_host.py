@@ -78,3 +78,12 @@ def test_reference_assembly_rule():
               "V0": np.ones((1, 3, 2)), "V1": np.ones((1, 3, 2))}
     h = orc.assemble(packed, np.array([0.0, 2.0]))
     assert np.allclose(h, 1 + 1 + 1 + 2)      # zero multiplier adds unscaled
+
+
+def test_f_functions_are_refused_by_the_gpu_build(gpu_free_lib):
+    """The device kernels are built for s, p, d; an f block is refused with
+    OLC_ERR_UNSUPPORTED before any device work (the oracle covers f)."""
+    from olcao_gb300 import api
+    with pytest.raises(api.OlcError) as e:
+        api.primitive_batch(1, np.zeros((1, 12)) + 1.0, np.array([[16, 1]], np.int32))
+    assert e.value.status == 7

@@ -82,11 +82,3 @@ def test_too_many_electrons_is_an_error(gpu_free_lib):
     with pytest.raises(api.OlcError):
         api.populate_states(np.zeros((2, 3)), np.full(2, 1.0), 7.0)
 
-
-def test_f_functions_are_refused_by_the_gpu_build(gpu_free_lib):
-    """The device kernels are built for s, p, d; an f block is refused with
-    OLC_ERR_UNSUPPORTED before any device work (the oracle covers f)."""
-    from olcao_gb300 import api
-    with pytest.raises(api.OlcError) as e:
-        api.primitive_batch(1, np.zeros((1, 12)) + 1.0, np.array([[16, 1]], np.int32))
-    assert e.value.status == 7
