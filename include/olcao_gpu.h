@@ -233,6 +233,15 @@ int olc_scf_matrices(olc_context_t* ctx, const double* coeffs, int kpoint,
 int olc_split_zgemm(olc_context_t* ctx, int m, int n, int k, const double* a,
                     const double* b, double* c);
 
+/* FP32-accurate complex product C = op(A) B (DEVICE complex64, column-major;
+ * op(A) = A (m x k, ld m) or, with conj_a, A^H of a k x m array (ld k)) from
+ * three BF16 pieces per operand on the tensor cores -- the product the
+ * mixed solver's FP32 stage uses for its reduction, back-transform and
+ * Loewdin steps.  No reference counterpart (the reference's products are
+ * LAPACK's FP64 BLAS); exposed for checking. */
+int olc_split_cgemm32(olc_context_t* ctx, int m, int n, int k, const float* a, int conj_a,
+                      const float* b, float* c);
+
 /* Stage timing (CUDA events on the context's stream) and kernel counting.
  * Stages: the integral primitives, the basis contraction, the Bloch sum and
  * scatter, the orthogonalisation (GEMMs + pack), Hamiltonian assembly, and
@@ -244,13 +253,21 @@ typedef enum {
   OLC_STAGE_ORTHO = 3,
   OLC_STAGE_ASSEMBLE = 4,
   OLC_STAGE_SOLVE = 5,
-  OLC_STAGE_REFINE = 6,        /* mixed precision: split products + extraction */
+  OLC_STAGE_REFINE = 6,        /* mixed precision: Loewdin step + cluster solves */
   OLC_STAGE_DENSITY = 7,       /* valence density and its traces               */
-  OLC_NUM_STAGES = 8
+  OLC_STAGE_TRIDIAG = 8,       /* mixed precision: FP32 tridiagonalisation      */
+  OLC_STAGE_BACKTRANSFORM = 9, /* mixed precision: reflector back-transform and X = U^-1 Z */
+  OLC_STAGE_SPLIT = 10,        /* mixed precision: FP64-accurate split products */
+  OLC_NUM_STAGES = 11
 } olc_stage_t;
 int olc_profile_enable(olc_context_t* ctx, int on);
 int olc_profile_reset(olc_context_t* ctx);
 int olc_profile_read(olc_context_t* ctx, int stage, int64_t* launches, double* ms);
+/* Algorithmic work of a stage since the last reset: tensor-core flops issued
+ * (the split and FP32-accurate products count every BF16 multiply-add) and
+ * the streamed bytes of the HBM-bound kernels (tridiagonalisation: the
+ * trailing triangle read and written at every step). */
+int olc_profile_read_work(olc_context_t* ctx, int stage, double* flops, double* bytes);
 /* Kernels of this library launched so far in the process (all contexts). */
 int64_t olc_launch_count(void);
 

@@ -47,11 +47,11 @@ EXPORTS = ("olc_version", "olc_last_error", "olc_create", "olc_destroy",
            "olc_ortho_pack", "olc_assemble_hamiltonian", "olc_solve_zhegv",
            "olc_scf_prepare", "olc_scf_iteration", "olc_primitive_batch",
            "olc_profile_enable", "olc_profile_reset", "olc_profile_read",
-           "olc_launch_count", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
-           "olc_split_zgemm", "olc_write_setup_integrals", "olc_write_eigen",
+           "olc_launch_count", "olc_profile_read_work", "olc_scf_matrices", "olc_solve_zhegv_noalloc",
+           "olc_split_zgemm", "olc_split_cgemm32", "olc_write_setup_integrals", "olc_write_eigen",
            "olc_make_valence_rho", "olc_populate_states")
 STAGES = ("primitives", "contract", "bloch", "ortho", "assemble", "solve", "refine",
-          "density")
+          "density", "tridiag", "backtransform", "split")
 
 _LIB: Optional[C.CDLL] = None
 
@@ -93,11 +93,13 @@ def lib() -> C.CDLL:
         L.olc_profile_enable.argtypes = [vp, i32]
         L.olc_profile_reset.argtypes = [vp]
         L.olc_profile_read.argtypes = [vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+        L.olc_profile_read_work.argtypes = [vp, i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         for name in EXPORTS[2:]:
             getattr(L, name).restype = C.c_int
         L.olc_scf_matrices.argtypes = [vp, dp, i32, dp, dp, i32]
         L.olc_solve_zhegv_noalloc.argtypes = [i32, i32, dp, dp, i32, dp, dp, dp, vp]
         L.olc_split_zgemm.argtypes = [vp, i32, i32, i32, dp, dp, dp]
+        L.olc_split_cgemm32.argtypes = [vp, i32, i32, i32, dp, i32, dp, dp]
         L.olc_write_setup_integrals.argtypes = [vp, C.c_char_p]
         L.olc_write_eigen.argtypes = [C.c_char_p, i32, i32, i32, i32, dp, dp]
         L.olc_make_valence_rho.argtypes = [vp, i32, i32, dp, dp, dp, dp, dp, dp]
@@ -245,6 +247,16 @@ class Context:
             out[name] = (int(n.value), float(ms.value))
         return out
 
+    def profile_work(self) -> Dict[str, Tuple[float, float]]:
+        """{stage: (tensor flops, streamed bytes)} since the last reset."""
+        out = {}
+        for i, name in enumerate(STAGES):
+            fl = C.c_double()
+            by = C.c_double()
+            _check(lib().olc_profile_read_work(self.h, i, C.byref(fl), C.byref(by)))
+            out[name] = (float(fl.value), float(by.value))
+        return out
+
     def set_stream(self, stream):
         _check(lib().olc_set_stream(self.h, C.c_void_p(stream.cuda_stream)))
 
@@ -335,6 +347,23 @@ class Context:
         Cc = torch.zeros(n, m, dtype=torch.complex128, device="cuda")
         _check(lib().olc_split_zgemm(self.h, m, n, k, Ac.data_ptr(), Bc.data_ptr(),
                                      Cc.data_ptr()))
+        return Cc.t()
+
+    def split_cgemm32(self, A, B, conj_a: bool = False):
+        """FP32-accurate complex product op(A) B on the tensor cores (device
+        complex64 tensors, row-major numpy-style; op(A) = A or A^H)."""
+        torch = self.torch
+        if conj_a:
+            k, m = A.shape
+        else:
+            m, k = A.shape
+        k2, n = B.shape
+        assert k == k2
+        Ac = A.t().contiguous()        # column-major storage of A
+        Bc = B.t().contiguous()
+        Cc = torch.zeros(n, m, dtype=torch.complex64, device="cuda")
+        _check(lib().olc_split_cgemm32(self.h, m, n, k, Ac.data_ptr(), int(conj_a), Bc.data_ptr(),
+                                       Cc.data_ptr()))
         return Cc.t()
 
     def scf_matrices(self, coeffs, k: int):

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libolcao_gb300.so")
 SOURCES = ["olc_capi.cpp", "olc_setup.cpp", "olc_integrals.cu", "olc_linalg.cu",
            "olc_eigen_small.cu", "olc_noalloc.cu", "olc_mixed.cu", "olc_tridiag.cu",
-           "olc_ozaki.cu", "olc_layout.cu", "olc_density.cu", "olc_populate.cpp"]
+           "olc_ozaki.cu", "olc_tcgemm.cu", "olc_layout.cu", "olc_density.cu", "olc_populate.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

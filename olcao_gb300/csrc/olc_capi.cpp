@@ -6,6 +6,7 @@
 #include <string>
 
 #include "olc_common.h"
+#include "olc_tcgemm.h"
 
 namespace olc {
 
@@ -102,6 +103,7 @@ int olc_last_error(char* buf, size_t len) {
 int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
   if (!out) return fail(OLC_ERR_ARG, "olc_create: null output");
   *out = nullptr;
+  if (!sys) return fail(OLC_ERR_ARG, "olc_create: null system");
   int dev = 0;
   int st = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   if (st) return st;
@@ -286,6 +288,20 @@ int olc_split_zgemm(olc_context_t* ctx, int m, int n, int k, const double* a, co
   return ozaki_selftest(ctx, m, n, k, a, b, c);
 }
 
+int olc_split_cgemm32(olc_context_t* ctx, int m, int n, int k, const float* a, int conj_a, const float* b,
+                      float* c) {
+  if (!ctx || !a || !b || !c || m < 1 || n < 1 || k < 1)
+    return fail(OLC_ERR_ARG, "olc_split_cgemm32: bad argument");
+  int st = tc::cgemm_f32(ctx, m, n, k, a, 0, conj_a ? k : m, conj_a != 0, b, 0, k, 1.0f, 0.0f, c, 0, m, 1,
+                         OLC_STAGE_REFINE);
+  int s2 = cuda_check(cudaStreamSynchronize(ctx->stream), "olc_split_cgemm32 sync");
+  if (st || s2) return st ? st : s2;
+  int code = 0;
+  if ((st = tc::read_error(&code))) return st;
+  if (code) return fail(OLC_ERR_CUDA, "tensor-core product: a pipeline wait expired");
+  return OLC_OK;
+}
+
 int olc_profile_enable(olc_context_t* ctx, int on) {
   if (!ctx) return fail(OLC_ERR_ARG, "olc_profile_enable: null context");
   ctx->profiling = on != 0;
@@ -298,6 +314,8 @@ int olc_profile_reset(olc_context_t* ctx) {
   for (int s = 0; s < OLC_NUM_STAGES; ++s) {
     ctx->prof_ms[s] = 0.0;
     ctx->prof_launches[s] = 0;
+    ctx->prof_flops[s] = 0.0;
+    ctx->prof_bytes[s] = 0.0;
   }
   return OLC_OK;
 }
@@ -307,6 +325,14 @@ int olc_profile_read(olc_context_t* ctx, int stage, int64_t* launches, double* m
   drain_profile(ctx);
   if (launches) *launches = ctx->prof_launches[stage];
   if (ms) *ms = ctx->prof_ms[stage];
+  return OLC_OK;
+}
+
+int olc_profile_read_work(olc_context_t* ctx, int stage, double* flops, double* bytes) {
+  if (!ctx || stage < 0 || stage >= OLC_NUM_STAGES)
+    return fail(OLC_ERR_ARG, "olc_profile_read_work: bad argument");
+  if (flops) *flops = ctx->prof_flops[stage];
+  if (bytes) *bytes = ctx->prof_bytes[stage];
   return OLC_OK;
 }
 

@@ -120,10 +120,11 @@ struct olc_context {
   double* g_coeff = nullptr;
   double* g_eig = nullptr;
   double* g_vec = nullptr;
-  // FP32 Cholesky factors of the prepared S(k) (they do not change between
-  // SCF passes): [nk][n][ld], valid after the first mixed pass
-  float* u32 = nullptr;
-  bool u32_valid = false;
+  // FP32 inverse Cholesky factors U^{-1} of the prepared S(k) (they do not
+  // change between SCF passes; FP64 factorisation): [nk][n][n], valid after
+  // the first mixed pass
+  float* w32 = nullptr;
+  bool w32_valid = false;
   // tuned CTAs per k of the FP32 tridiagonalisation (olc_tridiag.cu)
   int trd_tuned_n = 0, trd_tuned_nk = 0, trd_tuned_g = 0;
   cusolverDnHandle_t solver = nullptr;
@@ -177,6 +178,7 @@ struct olc_context {
   int mixed_n = 0;
   int mixed_lwork = 0;
   int* d_info = nullptr;
+  bool info_potrf = false;         // d_info holds potrf's info (else chegvd's)
   double* d_eval = nullptr;
   // profiling
   bool profiling = false;
@@ -184,6 +186,8 @@ struct olc_context {
   std::vector<cudaEvent_t> prof_pool;
   double prof_ms[OLC_NUM_STAGES] = {};
   int64_t prof_launches[OLC_NUM_STAGES] = {};
+  double prof_flops[OLC_NUM_STAGES] = {};
+  double prof_bytes[OLC_NUM_STAGES] = {};
 };
 
 namespace olc {
@@ -197,6 +201,13 @@ inline cudaError_t ctx_malloc(olc_context* ctx, void** p, size_t bytes, cudaStre
 
 void set_error(const std::string& msg);
 void count_launch(int n = 1);
+// Algorithmic work of a stage (tensor flops or streamed bytes), counted
+// while the context is profiling.
+inline void add_work(olc_context* ctx, int stage, double flops, double bytes) {
+  if (!ctx || !ctx->profiling || ctx->capturing) return;
+  ctx->prof_flops[stage] += flops;
+  ctx->prof_bytes[stage] += bytes;
+}
 
 // Records a stage's start on construction and its end on destruction when the
 // context is profiling; `launches` kernels are attributed to the stage.
@@ -298,7 +309,7 @@ int write_eigen(const char* root, int nk, int spin, int num_states, int vale_dim
 
 // batched FP32 eigen-solve (olc_tridiag.cu)
 int hetrd_max_n();
-int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X,
-                       const float* u_cached, float* u_store);
+int inverse_factors(olc_context* ctx, int n, int nk, const double* s64, float* w32);
+int solve_fp32_batched(olc_context* ctx, int n, int nk, const float* h32, const float* w32, float* X);
 
 }  // namespace olc

@@ -502,7 +502,7 @@ int scf_prepare(olc_context* ctx, int precision, int form) {
                             nullptr, ctx->d_h0, nullptr))) return st;
   }
   ctx->prepared = true;
-  ctx->u32_valid = false;
+  ctx->w32_valid = false;
   ctx->prep_precision = precision;
   ctx->prep_form = form;
   return cuda_check(cudaStreamSynchronize(ctx->stream), "prepare sync");

@@ -30,6 +30,7 @@
 #include <cuda_bf16.h>
 
 #include "olc_common.h"
+#include "olc_tcgemm.h"
 
 namespace olc {
 
@@ -72,15 +73,10 @@ struct ClusterLists {
 };
 
 // Per k (one CTA): a_j = Re Hh_jj (the basis is orthonormal after the Loewdin
-// step), sorted ascending; clusters are runs of consecutive values closer than
-// kClusterGap.  A run longer than kMaxCluster is cut into cores of at most
-// kMaxCore states at its widest gaps; a core is later solved together with
-// kBuffer neighbours on each cut side (only its own eigenpairs are kept), so
-// that the strongly coupled states across a cut are treated exactly.  Fills
-// the per-k arrays of L and appends every cluster except clean single states
-// to a work list.
-__global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict__ Hh, int n,
-                                                       ClusterLists L) {
+// step), sorted ascending (bitonic sort in shared memory); fills order, pos
+// and diag of L.
+__global__ void __launch_bounds__(1024) cluster_sort_kernel(const double* __restrict__ Hh, int n,
+                                                            ClusterLists L) {
   extern __shared__ double sortmem[];
   int P = 1;
   while (P < n) P <<= 1;
@@ -105,7 +101,8 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict_
         const int j = i ^ stride;
         if (j > i) {
           const bool up = (i & size) == 0;
-          if ((key[i] > key[j]) == up) {
+          const bool greater = key[i] > key[j] || (key[i] == key[j] && idx[i] > idx[j]);
+          if (greater == up) {
             const double t = key[i]; key[i] = key[j]; key[j] = t;
             const int u = idx[i]; idx[i] = idx[j]; idx[j] = u;
           }
@@ -117,40 +114,98 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const double* __restrict_
     L.order[(size_t)k * n + i] = idx[i];
     L.pos[(size_t)k * n + idx[i]] = i;
   }
-  if (tid == 0) {
-    // a cluster [s0, s1) with cut flags; clean singletons go to the warp kernel
-    auto close = [&](int s0, int s1, int flags) {
-      const int m = s1 - s0;
-      for (int s = s0; s < s1; ++s) L.csize[(size_t)k * n + s] = flags ? -m : m;
-      if (m > 1 || flags) {
-        const int ext = m + ((flags & 1) ? min(kBuffer, s0) : 0) + ((flags & 2) ? min(kBuffer, n - s1) : 0);
-        const bool sm = ext <= kSmallCluster;
-        const int at = atomicAdd(L.counters + (sm ? 0 : 1), 1);
-        if (at < L.cap) (sm ? L.small : L.large)[at] = make_int4(k, s0, m, flags);
-      }
-    };
-    int s0 = 0;
-    for (int i = 1; i <= n; ++i) {
-      if (i < n && key[i] - key[i - 1] < kClusterGap) continue;
-      // run [s0, i) of values closer than kClusterGap
-      if (i - s0 <= kMaxCluster) {
-        close(s0, i, 0);
-      } else {
-        // cores of at most kMaxCore states, each ending at the widest gap
-        // it can reach; cut sides are solved with buffer states
-        int cur = s0, cutl = 0;
-        while (i - cur > kMaxCore) {
-          int g = cur + 1;
-          for (int t = cur + 2; t <= cur + kMaxCore; ++t)
-            if (key[t] - key[t - 1] > key[g] - key[g - 1]) g = t;
-          close(cur, g, cutl | 2);
-          cur = g;
-          cutl = 1;
-        }
-        close(cur, i, cutl);
-      }
-      s0 = i;
+}
+
+// Strong couplings, one warp per (k, state p): the second-order fold treats
+// the coupling A_jp of p to a state j of another cluster only approximately
+// (its neglected terms grow with |A_jp| / |a_p - a_j|).  Where that ratio
+// exceeds kCoupleRatio (and |A_jp| exceeds kCoupleFloor) the two states must
+// be solved exactly in one cluster: reach[k][pos p] receives the largest
+// sorted slot of such a partner above p (integer maximum: the result does not
+// depend on the order of the warps).
+constexpr double kCoupleRatio = 1e-2;
+constexpr double kCoupleFloor = 1e-9;
+__global__ void __launch_bounds__(256) coupling_reach_kernel(const double* __restrict__ Hh, int n, int nk,
+                                                             ClusterLists L, int* __restrict__ reach) {
+  const int gw = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (gw >= n * nk) return;
+  const int k = gw / n, p = gw % n;
+  const size_t nn = (size_t)n * n;
+  const double* diag = L.diag + (size_t)k * n;
+  const int* pos = L.pos + (size_t)k * n;
+  const double ap = diag[p];
+  const int pp = pos[p];
+  const double* col = Hh + 2 * ((size_t)k * nn + (size_t)p * n);
+  int far = -1;
+  for (int j = lane; j < n; j += 32) {
+    const int pj = pos[j];
+    if (pj <= pp) continue;
+    const double ar = col[2 * j], ai = col[2 * j + 1];
+    const double a2 = ar * ar + ai * ai;
+    const double dlt = fabs(ap - diag[j]);
+    if (a2 > kCoupleFloor * kCoupleFloor && a2 > kCoupleRatio * kCoupleRatio * dlt * dlt) far = max(far, pj);
+  }
+  for (int o = 16; o; o >>= 1) far = max(far, __shfl_xor_sync(0xffffffffu, far, o));
+  if (lane == 0 && far >= 0) atomicMax(&reach[(size_t)k * n + pp], far);
+}
+
+// Clusters, one CTA per k (sorted values and reaches staged in shared memory,
+// one thread scans): runs of sorted values closer than kClusterGap,
+// joined across a boundary when a strong coupling (reach) crosses it.  A run
+// longer than kMaxCluster is cut into cores of at most kMaxCore states at its
+// widest gaps; a core is later solved together with kBuffer neighbours on
+// each cut side (only its own eigenpairs are kept), so that the strongly
+// coupled states across a cut are treated exactly.  Appends every cluster
+// except clean single states to a work list.
+__global__ void __launch_bounds__(256) cluster_form_kernel(int n, ClusterLists L, const int* __restrict__ reach) {
+  extern __shared__ double formmem[];
+  double* keys = formmem;
+  int* rk = reinterpret_cast<int*>(formmem + n);
+  const int k = blockIdx.x;
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    keys[s] = L.diag[(size_t)k * n + L.order[(size_t)k * n + s]];
+    rk[s] = reach[(size_t)k * n + s];
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  auto key = [&](int s) { return keys[s]; };
+  // a cluster [s0, s1) with cut flags; clean singletons go to the warp kernel
+  auto close = [&](int s0, int s1, int flags) {
+    const int m = s1 - s0;
+    for (int s = s0; s < s1; ++s) L.csize[(size_t)k * n + s] = flags ? -m : m;
+    if (m > 1 || flags) {
+      const int ext = m + ((flags & 1) ? min(kBuffer, s0) : 0) + ((flags & 2) ? min(kBuffer, n - s1) : 0);
+      const bool sm = ext <= kSmallCluster;
+      const int at = atomicAdd(L.counters + (sm ? 0 : 1), 1);
+      if (at < L.cap) (sm ? L.small : L.large)[at] = make_int4(k, s0, m, flags);
     }
+  };
+  int s0 = 0, span = rk[0];
+  for (int i = 1; i <= n; ++i) {
+    if (i < n && (key(i) - key(i - 1) < kClusterGap || span >= i)) {
+      span = max(span, rk[i]);
+      continue;
+    }
+    // run [s0, i)
+    if (i - s0 <= kMaxCluster) {
+      close(s0, i, 0);
+    } else {
+      // cores of at most kMaxCore states, each ending at the widest gap
+      // it can reach; cut sides are solved with buffer states
+      int cur = s0, cutl = 0;
+      while (i - cur > kMaxCore) {
+        int g = cur + 1;
+        for (int t = cur + 2; t <= cur + kMaxCore; ++t)
+          if (key(t) - key(t - 1) > key(g) - key(g - 1)) g = t;
+        close(cur, g, cutl | 2);
+        cur = g;
+        cutl = 1;
+      }
+      close(cur, i, cutl);
+    }
+    s0 = i;
+    if (i < n) span = rk[i];
   }
 }
 
@@ -581,51 +636,51 @@ __global__ void set_identity_kernel(double* __restrict__ S, int n, size_t total)
   }
 }
 
-__global__ void add_f32_inplace_kernel(float* __restrict__ X, const float* __restrict__ add,
-                                       size_t n2) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2;
-       i += (size_t)gridDim.x * blockDim.x)
-    X[i] += add[i];
-}
 
 }  // namespace
 
 // Hh := (I+F)^H Hh (I+F), Sh := I, X := X (I+F) with F = -E/2 + 3E^2/8, E = Sh - I.
+// The products with the small F run as FP32-accurate tensor-core products
+// (olc_tcgemm.cu): their relative error times |F| ~ 1e-5 is far below FP64
+// needs.
 int loewdin(olc_context* ctx, int n, int nk, double* Hh, double* Sh, float* X) {
   cudaStream_t stream = ctx->stream;
   const size_t nn = (size_t)n * n, total = nn * nk;
+  const long long s2 = 2 * (long long)nn;     // batch stride in floats
   float *E = nullptr, *F = nullptr, *H32 = nullptr, *T = nullptr;
   int st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&E, 8 * total, stream), "malloc E"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&F, 8 * total, stream), "malloc F"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&H32, 8 * total, stream), "malloc H32"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&T, 8 * total, stream), "malloc T"))) return st;
-  StageScope scope(ctx, OLC_STAGE_REFINE, 0);
-  loewdin_prep_kernel<<<grid_for(total), 256, 0, stream>>>(Hh, Sh, n, total, E, H32);
-  const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
-  auto* Ec = reinterpret_cast<cuComplex*>(E);
-  auto* Fc = reinterpret_cast<cuComplex*>(F);
-  auto* Hc = reinterpret_cast<cuComplex*>(H32);
-  auto* Tc = reinterpret_cast<cuComplex*>(T);
-  auto* Xc = reinterpret_cast<cuComplex*>(X);
-  const long long sn = (long long)nn;
-  auto gemm = [&](cublasOperation_t ta, const cuComplex* A, const cuComplex* B, cuComplex* C) {
-    return cublasCgemmStridedBatched(ctx->blas_f32, ta, CUBLAS_OP_N, n, n, n, &one, A, n, sn, B, n, sn,
-                                     &zero, C, n, sn, nk);
+  {
+    StageScope scope(ctx, OLC_STAGE_REFINE, 1);
+    loewdin_prep_kernel<<<grid_for(total), 256, 0, stream>>>(Hh, Sh, n, total, E, H32);
+  }
+  auto gemm = [&](const float* A, bool conjA, const float* B, float beta, float* C) {
+    return tc::cgemm_f32(ctx, n, n, n, A, s2, n, conjA, B, s2, n, 1.f, beta, C, s2, n, nk, OLC_STAGE_REFINE);
   };
-  if (gemm(CUBLAS_OP_N, Ec, Ec, Fc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm E^2 failed");
-  loewdin_f_kernel<<<grid_for(2 * total), 256, 0, stream>>>(E, F, 2 * total);
+  if ((st = gemm(E, false, E, 0.f, F))) return st;                 // F = E^2
+  {
+    StageScope scope(ctx, OLC_STAGE_REFINE, 1);
+    loewdin_f_kernel<<<grid_for(2 * total), 256, 0, stream>>>(E, F, 2 * total);
+  }
   // W = Hh + Hh F  (into Hh, FP32 copy into H32)
-  if (gemm(CUBLAS_OP_N, Hc, Fc, Tc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm HF failed");
-  add_f32_kernel<<<grid_for(2 * total), 256, 0, stream>>>(Hh, Hh, T, H32, 2 * total);
+  if ((st = gemm(H32, false, F, 0.f, T))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_REFINE, 1);
+    add_f32_kernel<<<grid_for(2 * total), 256, 0, stream>>>(Hh, Hh, T, H32, 2 * total);
+  }
   // Hh' = W + F^H W
-  if (gemm(CUBLAS_OP_C, Fc, Hc, Tc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm FW failed");
-  add_f32_kernel<<<grid_for(2 * total), 256, 0, stream>>>(Hh, Hh, T, nullptr, 2 * total);
-  // X' = X + X F
-  if (gemm(CUBLAS_OP_N, Xc, Fc, Tc) != CUBLAS_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cgemm XF failed");
-  add_f32_inplace_kernel<<<grid_for(2 * total), 256, 0, stream>>>(X, T, 2 * total);
-  set_identity_kernel<<<grid_for(total), 256, 0, stream>>>(Sh, n, total);
-  scope.add_launches(6);
+  if ((st = gemm(F, true, H32, 0.f, T))) return st;
+  {
+    StageScope scope(ctx, OLC_STAGE_REFINE, 2);
+    add_f32_kernel<<<grid_for(2 * total), 256, 0, stream>>>(Hh, Hh, T, nullptr, 2 * total);
+    set_identity_kernel<<<grid_for(total), 256, 0, stream>>>(Sh, n, total);
+  }
+  // X' = X + X F (the operand is split into BF16 pieces before the product
+  // writes, so X may be both operand and output)
+  if ((st = gemm(X, false, F, 1.f, X))) return st;
   cudaFreeAsync(E, stream);
   cudaFreeAsync(F, stream);
   cudaFreeAsync(H32, stream);
@@ -725,35 +780,46 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   int st;
   cudaStream_t stream = ctx->stream;
   // ---- 1. FP32 generalised solve per k -----------------------------------
-  // the prepared S(k) does not change between passes: its FP32 Cholesky
-  // factors are kept from the first pass
+  // W = U^{-1} (S = U^H U, FP64 factorisation rounded to FP32); the prepared
+  // S(k) does not change between passes, so its factors are kept from the
+  // first pass
   const bool batched = use_batched_fp32(n);
-  const bool cached = batched && s_prepared && ctx->u32_valid;
-  float *h32 = nullptr, *s32 = nullptr;
+  float* h32 = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
-  if (!cached && (st = cuda_check(ctx_malloc(ctx, (void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, cached ? 1 : 2);
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 1);
     to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
-    if (!cached) to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
   }
   float* X = nullptr;      // FP32 eigenvectors, [nk][n][n] complex
   if (batched) {
-    float* store = nullptr;
-    if (s_prepared && !cached) {
-      const size_t ld = (size_t)n + (n & 1);
-      if (!ctx->u32 && (st = dalloc(ctx, &ctx->u32, 2 * (size_t)n * ld * nk))) return st;
-      store = ctx->u32;
+    float* w32 = nullptr;
+    if (s_prepared) {
+      if (!ctx->w32 && (st = dalloc(ctx, &ctx->w32, 2 * nn * nk))) return st;
+      w32 = ctx->w32;
+      if (!ctx->w32_valid) {
+        if ((st = inverse_factors(ctx, n, nk, s, w32))) return st;
+        ctx->w32_valid = true;
+      } else if ((st = cuda_check(cudaMemsetAsync(ctx->d_info, 0, sizeof(int) * nk, stream), "clear info"))) {
+        return st;
+      }
+    } else {
+      if ((st = cuda_check(ctx_malloc(ctx, (void**)&w32, 8 * nn * nk, stream), "malloc w32"))) return st;
+      if ((st = inverse_factors(ctx, n, nk, s, w32))) return st;
     }
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
-    if ((st = solve_fp32_batched(ctx, n, nk, h32, s32, X, cached ? ctx->u32 : nullptr, store))) return st;
-    if (store) ctx->u32_valid = true;
+    if ((st = solve_fp32_batched(ctx, n, nk, h32, w32, X))) return st;
+    if (!s_prepared) cudaFreeAsync(w32, stream);
     cudaFreeAsync(h32, stream);
   } else {
+    float* s32 = nullptr;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
+    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
+    count_launch();
     if ((st = solve_fp32_library(ctx, n, nk, h32, s32))) return st;
+    ctx->info_potrf = false;
     X = h32;
+    cudaFreeAsync(s32, stream);
   }
-  if (s32) cudaFreeAsync(s32, stream);
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
   double *Y = nullptr, *Hh = nullptr, *Sh = nullptr;
   // bits kept of FP64 and FP32 operands (OLC_SPLIT_BITS overrides the FP64 count)
@@ -765,11 +831,15 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&Sh, 16ULL * nn * nk, stream), "malloc Sh"))) return st;
   const long long snn = (long long)nn * 2;
   // Y = H X ; Hh = X^H Y
-  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk))) return st;
-  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Hh, nk))) return st;
+  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk,
+                                       OLC_STAGE_SPLIT))) return st;
+  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Hh, nk,
+                                       OLC_STAGE_SPLIT))) return st;
   // Y = S X ; Sh = X^H Y
-  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, s, snn, n, false, b64, X, snn, n, b32, Y, nk))) return st;
-  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Sh, nk))) return st;
+  if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, s, snn, n, false, b64, X, snn, n, b32, Y, nk,
+                                       OLC_STAGE_SPLIT))) return st;
+  if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Sh, nk,
+                                       OLC_STAGE_SPLIT))) return st;
   cudaFreeAsync(Y, stream);
   // ---- 3. Loewdin transform: Sh = I + E  ->  (I+F)^H Hh (I+F), F = -E/2 + 3E^2/8
   // so that the pencil is standard; the products with the small F need only
@@ -787,18 +857,26 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.large, sizeof(int4) * (size_t)L.cap, stream), "malloc list"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&L.counters, 4 * sizeof(int), stream), "malloc counters"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&w_slot, 8ULL * n * nk, stream), "malloc w"))) return st;
+  int* reach = nullptr;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&reach, 4ULL * n * nk, stream), "malloc reach"))) return st;
   if (vectors && (st = cuda_check(ctx_malloc(ctx, (void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_REFINE, 4);
+    StageScope scope(ctx, OLC_STAGE_REFINE, 6);
     int P = 1;
     while (P < n) P <<= 1;
     const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
-    if ((st = cuda_check(cudaFuncSetAttribute(cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((st = cuda_check(cudaFuncSetAttribute(cluster_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sortmem), "smem attribute"))) return st;
     if ((st = cuda_check(cudaFuncSetAttribute(final_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sortmem), "smem attribute"))) return st;
     if ((st = cuda_check(cudaMemsetAsync(L.counters, 0, 4 * sizeof(int), stream), "memset"))) return st;
-    cluster_kernel<<<nk, 1024, sortmem, stream>>>(Hh, n, L);
+    cluster_sort_kernel<<<nk, 1024, sortmem, stream>>>(Hh, n, L);
+    if ((st = cuda_check(cudaMemsetAsync(reach, 0xff, 4ULL * n * nk, stream), "memset reach"))) return st;
+    coupling_reach_kernel<<<(int)(((size_t)n * nk * 32 + 255) / 256), 256, 0, stream>>>(Hh, n, nk, L, reach);
+    const size_t formmem = (size_t)n * (sizeof(double) + sizeof(int));
+    if ((st = cuda_check(cudaFuncSetAttribute(cluster_form_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)formmem), "smem attribute"))) return st;
+    cluster_form_kernel<<<nk, 256, formmem, stream>>>(n, L, reach);
     singleton_kernel<<<(int)(((size_t)n * nk * 32 + 255) / 256), 256, 0, stream>>>(Hh, X, L, n, nk, w_slot,
                                                                                   v_slot);
     const size_t sm_small = sizeof(ClusterSmem<kSmallCluster>), sm_large = sizeof(ClusterSmem<kMaxCluster>);
@@ -830,6 +908,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   cudaFreeAsync(L.large, stream);
   cudaFreeAsync(L.counters, stream);
   cudaFreeAsync(w_slot, stream);
+  cudaFreeAsync(reach, stream);
   if (v_slot) cudaFreeAsync(v_slot, stream);
   cudaFreeAsync(Hh, stream);
   cudaFreeAsync(Sh, stream);
@@ -847,8 +926,11 @@ int mixed_check_info(olc_context* ctx) {
   int st = cuda_check(cudaStreamSynchronize(ctx->stream), "mixed solve sync");
   if (st) return st;
   for (int k = 0; k < nk; ++k) {
-    if (hinfo[k] != 0) ctx->u32_valid = false;
-    if (hinfo[k] > n) return fail(OLC_ERR_NOT_PD, "overlap matrix not positive definite (FP32 factorisation)");
+    if (hinfo[k] != 0) ctx->w32_valid = false;
+    // potrf: info in 1..n = leading minor not positive definite; chegvd:
+    // info > n the same, info <= n = no convergence
+    if (hinfo[k] > n || (hinfo[k] > 0 && ctx->info_potrf))
+      return fail(OLC_ERR_NOT_PD, "overlap matrix not positive definite");
     if (hinfo[k] != 0) return fail(OLC_ERR_EIGEN, "FP32 eigen-solver did not converge");
   }
   return OLC_OK;

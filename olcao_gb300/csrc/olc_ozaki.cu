@@ -23,7 +23,11 @@
 #include <algorithm>
 #include <cuda_bf16.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include "olc_common.h"
+#include "olc_tcgemm.h"
 
 namespace olc {
 
@@ -257,6 +261,11 @@ template <class TA, class TB>
 int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
                 int nb, int stage) {
+  // the hand-written tcgen05 kernel (olc_tcgemm.cu) unless OLC_SPLIT_GEMM=cublas
+  // selects the library GEMM path below
+  const char* path = std::getenv("OLC_SPLIT_GEMM");
+  if (!(path && std::strcmp(path, "cublas") == 0))
+    return tc::zgemm_fixed<TA, TB>(ctx, m, n, k, A, sA, lda, conjA, bits_a, B, sB, ldb, bits_b, C, nb, stage);
   cudaStream_t st = ctx->stream;
   int beta, na, nbs;
   ozaki_plan(k, bits_a, bits_b, &beta, &na, &nbs);

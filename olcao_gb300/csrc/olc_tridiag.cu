@@ -2,8 +2,10 @@
 // stage of the mixed-precision solver (the role LAPACK chegv plays, restated
 // for one GPU and all k-points together).
 //
-//   1. S = U^H U (cuSOLVER potrfBatched) and C = U^{-H} H U^{-1} (two cuBLAS
-//      batched triangular solves).
+//   1. C = W^H H W with W = U^{-1}, S = U^H U: W comes from
+//      inverse_factors (FP64 Cholesky and triangular inverse, rounded to
+//      FP32, computed once per prepared S); the two products run on the
+//      tensor cores (three BF16 pieces per FP32 operand, olc_tcgemm.cu).
 //   2. C = Q T Q^H by Householder reflectors H_i = I - tau_i v_i v_i^H, the
 //      lower-triangle reduction of LAPACK chetd2: one thread-block cluster per
 //      k owns the k's matrix in HBM, its CTAs own interleaved columns.  Every
@@ -17,9 +19,9 @@
 //      T - sigma I, as LAPACK dstein), then modified Gram-Schmidt inside every
 //      group of eigenvalues too close for inverse iteration to separate.
 //   4. Back-transform Z = Q Z_T in blocks of 128 reflectors written as
-//      I - V T V^H (compact WY, LAPACK clarft), three strided-batched GEMMs
-//      per block.
-//   5. X = U^{-1} Z (cuBLAS batched triangular solve).
+//      I - V T V^H (compact WY, LAPACK clarft), four tensor-core products per
+//      block.
+//   5. X = W Z (tensor-core product).
 // X is S-orthonormal and diagonalises H to FP32 accuracy; the Rayleigh-Ritz
 // step of the mixed solver takes it from there.
 #include <algorithm>
@@ -30,6 +32,7 @@
 #include <vector>
 
 #include "olc_common.h"
+#include "olc_tcgemm.h"
 
 namespace cg = cooperative_groups;
 
@@ -100,18 +103,45 @@ __device__ __forceinline__ void block_sum2_d(double& a, double& b, double* red) 
 // together with the shares of p^H v_i, and w_i = p - tau_i/2 (p^H v_i) v_i
 // becomes the pending update; the owner of column i stores v_i there.  Two
 // cluster barriers per step.
+//
+// Deterministic variant (DET): the partial products are accumulated in
+// 64-bit fixed point with integer shared-memory atomics, whose sum does not
+// depend on the order in which the warps add; the unit of step i is
+// 2^-60 of a bound on every partial sum, ||A||_F ||v_i|| (the Frobenius norm
+// of the whole matrix bounds the trailing one: the reflectors are unitary).
+// A rerun gives bit-identical reflectors.  It needs 40 bytes of shared
+// memory per row (the float variant 32), so the largest n run the float
+// variant.
 constexpr int kTrdPanel = 8;      // owned columns per warp and pass
+
+// Destination of the partial products A v_i of one CTA.
+struct TrdAcc {
+  float2* w;                      // float variant: shared-memory float sums
+  unsigned long long* q;          // DET: fixed-point sums [2 * row] (re, im)
+  float scale;                    // DET: 1 / unit (a power of two)
+};
+
+template <bool DET>
+__device__ __forceinline__ void acc_add(const TrdAcc& a, int c, float x, float y) {
+  if (DET) {
+    atomicAdd(&a.q[2 * c], (unsigned long long)__float2ll_rn(x * a.scale));
+    atomicAdd(&a.q[2 * c + 1], (unsigned long long)__float2ll_rn(y * a.scale));
+  } else {
+    atomicAdd(&a.w[c].x, x);
+    atomicAdd(&a.w[c].y, y);
+  }
+}
 
 // One row pair (2q, 2q+1) of a panel: pending update, write-back, column
 // products and the pair's mirrored products.  MASK: the pair may lie on or
 // above a panel column's diagonal.
-template <bool PEND, bool MASK>
+template <bool DET, bool PEND, bool MASK>
 __device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int ld, int q,
                                          const int (&cr)[kTrdPanel], const float2* __restrict__ vP,
                                          const float2* __restrict__ wP, const float2 (&vr)[kTrdPanel],
                                          float (&ax)[kTrdPanel], float (&ay)[kTrdPanel],
                                          const float4* __restrict__ vP4, const float4* __restrict__ wP4,
-                                         const float4* __restrict__ vC4, float2* wC) {
+                                         const float4* __restrict__ vC4, const TrdAcc& wC) {
   const int c0 = 2 * q;
   float4 a4[kTrdPanel];
 #pragma unroll
@@ -156,22 +186,16 @@ __device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int ld,
       s1y += a1.x * vr[t].y + a1.y * vr[t].x;
     }
   }
-  if (!MASK || s0x != 0.f || s0y != 0.f) {
-    atomicAdd(&wC[c0].x, s0x);
-    atomicAdd(&wC[c0].y, s0y);
-  }
-  if (!MASK || s1x != 0.f || s1y != 0.f) {
-    atomicAdd(&wC[c0 + 1].x, s1x);
-    atomicAdd(&wC[c0 + 1].y, s1y);
-  }
+  if (!MASK || s0x != 0.f || s0y != 0.f) acc_add<DET>(wC, c0, s0x, s0y);
+  if (!MASK || s1x != 0.f || s1y != 0.f) acc_add<DET>(wC, c0 + 1, s1x, s1y);
 }
 
 // One panel of kTrdPanel owned columns (slots past the last column are
 // empty): the pairs touching the diagonals first, then the bulk unmasked.
-template <bool PEND>
+template <bool DET, bool PEND>
 __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld, int r0, int G, int pn, int nown,
                                           int lane, const float2* vP, const float2* wP, const float2* vC,
-                                          float2* wC) {
+                                          const TrdAcc& wC) {
   int cr[kTrdPanel];
   float2 vr[kTrdPanel];
   float ax[kTrdPanel], ay[kTrdPanel];
@@ -192,8 +216,8 @@ __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld
   const int q1 = ld >> 1;                       // the last pair may hold the zero padding row
   const int qd = min(q1, (c_last >> 1) + 1);    // pairs from qd on lie below every diagonal
   int q = (cr[0] >> 1) + lane;
-  for (; q < qd; q += 32) trd_pair<PEND, true>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
-  for (; q < q1; q += 32) trd_pair<PEND, false>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+  for (; q < qd; q += 32) trd_pair<DET, PEND, true>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+  for (; q < q1; q += 32) trd_pair<DET, PEND, false>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
     float x = ax[t], y = ay[t];
@@ -201,13 +225,11 @@ __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld
       x += __shfl_xor_sync(0xffffffffu, x, o);
       y += __shfl_xor_sync(0xffffffffu, y, o);
     }
-    if (lane == 0 && cr[t] < n) {
-      atomicAdd(&wC[cr[t]].x, x);
-      atomicAdd(&wC[cr[t]].y, y);
-    }
+    if (lane == 0 && cr[t] < n) acc_add<DET>(wC, cr[t], x, y);
   }
 }
 
+template <bool DET>
 __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__ A, int n, int ld,
                                                             double* __restrict__ dout,
                                                             double* __restrict__ eout,
@@ -220,20 +242,52 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
   float2* Ak = A + (size_t)k * n * ld;
   extern __shared__ float4 trd_sm4[];
   float2* trd_sm = reinterpret_cast<float2*>(trd_sm4);
+  // float variant: [v_a | w_a | v_b | w_b], (v, w) pairs alternating between steps;
+  // DET: [v_a | v_b | w | fixed-point sums (2 ld int64)]
+  unsigned long long* qsum = reinterpret_cast<unsigned long long*>(trd_sm + 3 * (size_t)ld);
   __shared__ double red[72];
   __shared__ float2 s_tau, s_scale;
-  __shared__ float s_diag, s_beta;
+  __shared__ float s_diag, s_beta, s_qscale;
+  __shared__ double s_unit, s_fro;
   __shared__ double2 s_dot[16];
-  for (int e = tid; e < 4 * ld; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
+  for (int e = tid; e < (DET ? 5 : 4) * ld; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
+  if (DET) {
+    // ||A||_F of the lower-triangle storage (off-diagonal entries twice)
+    double part = 0.0;
+    for (int c = rank; c < n; c += G) {
+      const float2* col = Ak + (size_t)c * ld;
+      for (int r = c + tid; r < n; r += blockDim.x) {
+        const float2 a = col[r];
+        part += (r == c ? 1.0 : 2.0) * ((double)a.x * a.x + (double)a.y * a.y);
+      }
+    }
+    const double f2 = block_sum_d(part, red);
+    if (tid == 0)
+      for (int g = 0; g < G; ++g) cl.map_shared_rank(s_dot, g)[rank] = make_double2(f2, 0.0);
+  }
   __syncthreads();
   cl.sync();
+  if (DET && tid == 0) {
+    double f2 = 0.0;
+    for (int g = 0; g < G; ++g) f2 += s_dot[g].x;
+    s_fro = sqrt(f2);
+  }
   int cur = 0;
   bool pend = false;
   for (int i = 0; i < n - 1; ++i) {
-    float2* vC = trd_sm + (size_t)(2 * cur) * ld;        // v_i
-    float2* wC = trd_sm + (size_t)(2 * cur + 1) * ld;    // partial A v_i, then w_i
-    const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * ld;   // pending v_{i-1}
-    float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;     // pending w_{i-1}
+    float2 *vC, *wC, *wP;
+    const float2* vP;
+    if (DET) {
+      vC = trd_sm + (size_t)cur * ld;                  // v_i
+      vP = trd_sm + (size_t)(1 - cur) * ld;            // pending v_{i-1}
+      wP = trd_sm + 2 * (size_t)ld;                    // pending w_{i-1}, then w_i
+      wC = wP;
+    } else {
+      vC = trd_sm + (size_t)(2 * cur) * ld;            // v_i
+      wC = trd_sm + (size_t)(2 * cur + 1) * ld;        // partial A v_i, then w_i
+      vP = trd_sm + (size_t)(2 * (1 - cur)) * ld;      // pending v_{i-1}
+      wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;  // pending w_{i-1}
+    }
     // ---- (a) every CTA: pending update of column i, reflector of column i ----
     // (column i is read from L2 by all CTAs; its owner writes v_i back only
     // after the next cluster barrier)
@@ -258,16 +312,26 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
         const float2 al = vC[i + 1];
         float2 tau = make_float2(0.f, 0.f), scale = make_float2(0.f, 0.f);
         float beta = al.x;
+        double vnorm2 = 1.0;
         if (!(xn2 == 0.0 && al.y == 0.f)) {
           const float an = sqrtf(al.x * al.x + al.y * al.y + (float)xn2);
           beta = (al.x >= 0.f) ? -an : an;
           tau = make_float2((beta - al.x) / beta, -al.y / beta);
           const float dr = al.x - beta, di = al.y, den = dr * dr + di * di;
           scale = make_float2(dr / den, -di / den);
+          vnorm2 = 1.0 + xn2 / (double)den;
         }
         s_tau = tau;
         s_scale = scale;
         s_beta = beta;
+        if (DET) {
+          // unit 2^(E - 60) with 2^E >= 2 ||A||_F ||v_i||
+          int E;
+          frexp(2.0 * s_fro * sqrt(vnorm2) + 1e-300, &E);
+          E = max(E, -60);
+          s_unit = ldexp(1.0, E - 60);
+          s_qscale = ldexpf(1.f, 60 - E);
+        }
       }
       __syncthreads();
       const float2 scale = s_scale;
@@ -283,11 +347,12 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       // panels of kTrdPanel owned columns per warp; lane-owned row pairs
       // (2q, 2q+1) collect the mirrored products of the whole panel in
       // registers before one shared-memory atomic
+      const TrdAcc acc{wC, qsum, DET ? s_qscale : 1.f};
       const int nown = r0 < n ? (n - r0 + G - 1) / G : 0;
       const int npanel = (nown + kTrdPanel - 1) / kTrdPanel;
       for (int pn = warp; pn < npanel; pn += nwarps) {
-        if (pend) trd_panel<true>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, wC);
-        else trd_panel<false>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, wC);
+        if (pend) trd_panel<DET, true>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, acc);
+        else trd_panel<DET, false>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, acc);
       }
     }
     __syncthreads();
@@ -298,12 +363,23 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
       int c0 = i + 1;
       c0 += ((rank - c0) % G + G) % G;
       double sx = 0.0, sy = 0.0;
+      const double unit = DET ? s_unit : 0.0;
       for (int c = c0 + tid * G; c < n; c += blockDim.x * G) {
         float2 t = make_float2(0.f, 0.f);
-        for (int g = 0; g < G; ++g) {
-          const float2 u = cl.map_shared_rank(wC, g)[c];
-          t.x += u.x;
-          t.y += u.y;
+        if (DET) {
+          long long qr = 0, qi = 0;      // integer sums: the same in any order
+          for (int g = 0; g < G; ++g) {
+            const unsigned long long* qg = cl.map_shared_rank(qsum, g);
+            qr += (long long)qg[2 * c];
+            qi += (long long)qg[2 * c + 1];
+          }
+          t = make_float2((float)((double)qr * unit), (float)((double)qi * unit));
+        } else {
+          for (int g = 0; g < G; ++g) {
+            const float2 u = cl.map_shared_rank(wC, g)[c];
+            t.x += u.x;
+            t.y += u.y;
+          }
         }
         t = cmul(tau, t);
         const float2 v = vC[c];
@@ -326,7 +402,15 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
         wC[c].x += t.x;
         wC[c].y += t.y;
       }
-      for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
+      if (DET) {
+        // every CTA has read this CTA's sums (cluster barrier above)
+        for (int c = i + tid; c < n; c += blockDim.x) {
+          qsum[2 * c] = 0ULL;
+          qsum[2 * c + 1] = 0ULL;
+        }
+      } else {
+        for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
+      }
       // the owner stores the reflector and T's entries
       if (rank == i % G) {
         float2* col = Ak + (size_t)i * ld;
@@ -347,8 +431,8 @@ __global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__
   if (rank == last % G && tid == 0) {
     float2 a = Ak[(size_t)last * ld + last];
     if (pend) {
-      const float2* vP = trd_sm + (size_t)(2 * (1 - cur)) * ld;
-      const float2* wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;
+      const float2* vP = DET ? trd_sm + (size_t)(1 - cur) * ld : trd_sm + (size_t)(2 * (1 - cur)) * ld;
+      const float2* wP = DET ? trd_sm + 2 * (size_t)ld : trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;
       const float2 t1 = cmul(vP[last], conjf2(wP[last])), t2 = cmul(wP[last], conjf2(vP[last]));
       a.x -= t1.x + t2.x;
     }
@@ -646,34 +730,38 @@ __global__ void tfactor_kernel(const float2* __restrict__ Gm, const float2* __re
   }
 }
 
-// [nk] matrices of n columns: leading dimension ld_in -> ld_out (rows
-// beyond n zero).
-__global__ void relayout_kernel(const float2* __restrict__ in, int n, int ld_in, int ld_out, int nk,
-                                float2* __restrict__ out) {
-  const size_t total = (size_t)nk * n * ld_out;
+// Upper triangle of the FP64 factor (row-major-free: column-major [nk][n][n])
+// rounded to FP32, the strictly lower part zero (potrf and trtri leave the
+// input's lower triangle in place).
+__global__ void upper_to_f32_kernel(const double* __restrict__ in, int n, size_t total, float* __restrict__ out) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
-    const int r = (int)(e % ld_out);
-    const size_t cb = e / ld_out;             // k * n + column
-    out[e] = r < n ? in[cb * ld_in + r] : make_float2(0.f, 0.f);
+    const size_t r2 = e % ((size_t)n * n);
+    const int r = (int)(r2 % n), c = (int)(r2 / n);
+    out[2 * e] = r <= c ? (float)in[2 * e] : 0.f;
+    out[2 * e + 1] = r <= c ? (float)in[2 * e + 1] : 0.f;
   }
-}
-
-__global__ void ptr_array_kernel(float2* base, size_t stride, int nk, float2** out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < nk) out[k] = base + (size_t)k * stride;
 }
 
 }  // namespace
 
-int hetrd_max_n() {
+static int max_smem_optin() {
   int dev = 0, smem = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return (smem - 2048) / (4 * (int)sizeof(float2));
+  return smem;
 }
 
-// One tridiagonalisation launch with clusters of G CTAs (one cluster per k).
+int hetrd_max_n() { return (max_smem_optin() - 2048) / (4 * (int)sizeof(float2)); }
+
+// Shared memory of the tridiagonalisation: 32 (float) or 40 (DET) bytes per row.
+static size_t hetrd_smem(int ld, bool det) { return (det ? 40 : 32) * (size_t)ld; }
+
+// The deterministic variant wherever its shared memory fits.
+static bool hetrd_det(int ld) { return hetrd_smem(ld, true) + 2048 <= (size_t)max_smem_optin(); }
+
+// One tridiagonalisation launch with clusters of G CTAs (one cluster per k);
+// G = 16 is a non-portable cluster size (allowed explicitly).
 static int launch_hetrd(olc_context* ctx, int G, float2* H, int n, int ld, int nk, size_t smem, double* d,
                         double* e, float2* tau) {
   cudaLaunchConfig_t cfg = {};
@@ -688,7 +776,33 @@ static int launch_hetrd(olc_context* ctx, int G, float2* H, int n, int ld, int n
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel, H, n, ld, d, e, tau), "hetrd launch");
+  if (hetrd_det(ld))
+    return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel<true>, H, n, ld, d, e, tau), "hetrd launch");
+  return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel<false>, H, n, ld, d, e, tau), "hetrd launch");
+}
+
+// Whether clusters of G CTAs of this kernel with this shared memory can be
+// resident at all (16 exceeds the portable limit and may not fit a GPC).
+static bool cluster_fits(int G, int ld, size_t smem) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(G, 1, 1);
+  cfg.blockDim = dim3(kTrdThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  const cudaError_t r = hetrd_det(ld) ? cudaOccupancyMaxActiveClusters(&nclusters, hetrd_kernel<true>, &cfg)
+                                      : cudaOccupancyMaxActiveClusters(&nclusters, hetrd_kernel<false>, &cfg);
+  if (r != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return nclusters > 0;
 }
 
 // Autotuner of the CTAs per k: the first pass of a context for a given
@@ -700,9 +814,9 @@ static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk
     *G = ctx->trd_tuned_g;
     return OLC_OK;
   }
-  int cand[4], nc = 0;
-  for (int g = 1; g <= 8; g *= 2)
-    if (g * nk <= 2 * 152 && (g * nk >= 38 || g == 8)) cand[nc++] = g;
+  int cand[5], nc = 0;
+  for (int g = 1; g <= 16; g *= 2)
+    if (g * nk <= 2 * 152 && (g * nk >= 38 || g == 8) && cluster_fits(g, ld, smem)) cand[nc++] = g;
   if (!nc) cand[nc++] = 1;
   int best = cand[0];
   if (nc > 1) {
@@ -738,70 +852,93 @@ static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk
   return OLC_OK;
 }
 
+// W = U^{-1} (S = U^H U) of every k in FP64 -- the Cholesky factorisation
+// of S(k) stays in FP64 because diffuse Gaussians make S ill-conditioned --
+// rounded to FP32 into w32 ([nk][n][n] complex, upper triangular).
+// ctx->d_info receives potrf's info per k (> 0: not positive definite).
+// s64: full Hermitian FP64 [nk][n][n], not modified.
+int inverse_factors(olc_context* ctx, int n, int nk, const double* s64, float* w32) {
+  cudaStream_t stream = ctx->stream;
+  const size_t nn = (size_t)n * n;
+  int st;
+  double* Sd = nullptr;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&Sd, 16 * nn * nk, stream), "malloc FP64 factor"))) return st;
+  if ((st = cuda_check(cudaMemcpyAsync(Sd, s64, 16 * nn * nk, cudaMemcpyDeviceToDevice, stream), "copy S")))
+    return st;
+  if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
+  StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
+  cusolverDnSetStream(ctx->solver, stream);
+  cusolverDnParams_t params;
+  if (cusolverDnCreateParams(&params) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolver params");
+  size_t dws = 0, hws = 0, dws2 = 0, hws2 = 0;
+  if (cusolverDnXpotrf_bufferSize(ctx->solver, params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, Sd, n, CUDA_C_64F,
+                                  &dws, &hws) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnXtrtri_bufferSize(ctx->solver, CUBLAS_FILL_MODE_UPPER, CUBLAS_DIAG_NON_UNIT, n, CUDA_C_64F, Sd, n,
+                                  &dws2, &hws2) != CUSOLVER_STATUS_SUCCESS) {
+    cusolverDnDestroyParams(params);
+    return fail(OLC_ERR_CUDA, "potrf/trtri buffer size");
+  }
+  dws = std::max(dws, dws2);
+  hws = std::max(hws, hws2);
+  void* dwork = nullptr;
+  int* tinfo = nullptr;        // trtri's info (cannot fail after a successful potrf)
+  std::vector<char> hwork(std::max<size_t>(hws, 1));
+  if ((st = cuda_check(ctx_malloc(ctx, &dwork, std::max<size_t>(dws, 16), stream), "malloc factor work")) ||
+      (st = cuda_check(ctx_malloc(ctx, (void**)&tinfo, sizeof(int) * nk, stream), "malloc trtri info"))) {
+    cusolverDnDestroyParams(params);
+    return st;
+  }
+  for (int k = 0; k < nk && !st; ++k) {
+    double* Ak = Sd + 2 * nn * k;
+    if (cusolverDnXpotrf(ctx->solver, params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, Ak, n, CUDA_C_64F, dwork, dws,
+                         hwork.data(), hws, ctx->d_info + k) != CUSOLVER_STATUS_SUCCESS)
+      st = fail(OLC_ERR_CUDA, "cusolverDnXpotrf failed");
+    else if (cusolverDnXtrtri(ctx->solver, CUBLAS_FILL_MODE_UPPER, CUBLAS_DIAG_NON_UNIT, n, CUDA_C_64F, Ak, n, dwork,
+                              dws, hwork.data(), hws, tinfo + k) != CUSOLVER_STATUS_SUCCESS)
+      st = fail(OLC_ERR_CUDA, "cusolverDnXtrtri failed");
+  }
+  // d_info keeps potrf's info: a failed factor is refused by mixed_check_info
+  ctx->info_potrf = true;
+  cusolverDnDestroyParams(params);
+  if (st) return st;
+  upper_to_f32_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(Sd, n, nn * nk,
+                                                                                                 w32);
+  scope.add_launches(1);
+  cudaFreeAsync(dwork, stream);
+  cudaFreeAsync(tinfo, stream);
+  cudaFreeAsync(Sd, stream);
+  return cuda_check(cudaGetLastError(), "inverse factors");
+}
+
 // FP32 eigenvectors X (S-orthonormal, [nk][n][n] complex column-major) of
-// every pencil (h32, s32).  h32 and s32 are overwritten (reduced matrix and
-// reflectors; Cholesky factor).  ctx->d_info receives potrf's info per k.
-// s32 may be null when u_cached holds the factors (layout [nk][n][ld],
-// ld = n rounded up to even); u_store, when given, receives the factors.
-int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, float* X,
-                       const float* u_cached, float* u_store) {
+// every pencil (h32, S) with w32 = U^{-1} from inverse_factors.  h32 is not
+// modified.
+int solve_fp32_batched(olc_context* ctx, int n, int nk, const float* h32, const float* w32, float* X) {
   cudaStream_t stream = ctx->stream;
   int st;
   if (n < 2) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver needs n >= 2");
   if (n > hetrd_max_n()) return fail(OLC_ERR_UNSUPPORTED, "batched FP32 solver: n above the shared-memory limit");
-  // columns padded to an even length (a zero row) so that every column
-  // starts on a 16-byte boundary; nn = batch stride
+  // the reduced matrix and the tridiagonal eigenvectors keep columns of even
+  // length (a zero row for odd n) so that every column starts on a 16-byte
+  // boundary; nn = batch stride of those, n2 = batch stride of h32, w32, X
   const int ld = n + (n & 1);
-  const size_t nn = (size_t)n * ld;
-  float2 *H = reinterpret_cast<float2*>(h32), *Sm = reinterpret_cast<float2*>(s32);
-  float2* Xc = reinterpret_cast<float2*>(X);
-  float2* Sq_alloc = nullptr;
-  if (ld != n) {
-    float2 *Hq = nullptr, *Sq = nullptr, *Xq = nullptr;
-    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Hq, 8 * nn * nk, stream), "malloc padded H"))) return st;
-    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Sq, 8 * nn * nk, stream), "malloc padded S"))) return st;
-    if ((st = cuda_check(ctx_malloc(ctx, (void**)&Xq, 8 * nn * nk, stream), "malloc padded X"))) return st;
-    relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, n, ld, nk, Hq);
-    if (!u_cached)
-      relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(Sm, n, n, ld, nk, Sq);
-    count_launch(2);
-    H = Hq;
-    Sm = Sq;
-    Sq_alloc = Sq;
-    Xc = Xq;
-  }
-  float2** ptrs = nullptr;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&ptrs, sizeof(float2*) * 3 * nk, stream), "malloc ptrs"))) return st;
-  if (u_cached) Sm = const_cast<float2*>(reinterpret_cast<const float2*>(u_cached));
-  ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Sm, nn, nk, ptrs);
-  ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(H, nn, nk, ptrs + nk);
-  ptr_array_kernel<<<(nk + 127) / 128, 128, 0, stream>>>(Xc, nn, nk, ptrs + 2 * nk);
-  const cuComplex one = make_cuComplex(1.f, 0.f), mone = make_cuComplex(-1.f, 0.f),
-                  zero = make_cuComplex(0.f, 0.f);
-  auto** Sp = reinterpret_cast<cuComplex**>(ptrs);
-  auto** Hp = reinterpret_cast<cuComplex**>(ptrs + nk);
-  auto** Xp = reinterpret_cast<cuComplex**>(ptrs + 2 * nk);
-  // ---- 1. Cholesky and reduction ------------------------------------------
-  {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
-    cusolverDnSetStream(ctx->solver, stream);
-    if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
-    if (!u_cached) {
-      if (cusolverDnCpotrfBatched(ctx->solver, CUBLAS_FILL_MODE_UPPER, n, Sp, ld, ctx->d_info, nk) !=
-          CUSOLVER_STATUS_SUCCESS)
-        return fail(OLC_ERR_CUDA, "cusolverDnCpotrfBatched failed");
-      if (u_store)
-        cudaMemcpyAsync(u_store, Sm, sizeof(float2) * nn * nk, cudaMemcpyDeviceToDevice, stream);
-    } else {
-      cudaMemsetAsync(ctx->d_info, 0, sizeof(int) * nk, stream);
-    }
-    if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Hp, ld, nk) != CUBLAS_STATUS_SUCCESS)
-      return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-H H) failed");
-    if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Hp, ld, nk) != CUBLAS_STATUS_SUCCESS)
-      return fail(OLC_ERR_CUDA, "ctrsmBatched (H U^-1) failed");
-  }
+  const size_t nn = (size_t)n * ld, n2 = (size_t)n * n;
+  float2 *C = nullptr, *Zc = nullptr;
+  float* T = nullptr;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&C, 8 * nn * nk, stream), "malloc reduced matrix"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&Zc, 8 * nn * nk, stream), "malloc Z"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&T, 8 * n2 * nk, stream), "malloc H W"))) return st;
+  if (ld != n && (st = cuda_check(cudaMemsetAsync(C, 0, 8 * nn * nk, stream), "clear padding"))) return st;
+  // ---- 1. C = W^H (H W) ------------------------------------------------------
+  if ((st = tc::cgemm_f32(ctx, n, n, n, h32, 2 * (long long)n2, n, false, w32, 2 * (long long)n2, n, 1.f, 0.f, T,
+                          2 * (long long)n2, n, nk, OLC_STAGE_SOLVE)))
+    return st;
+  if ((st = tc::cgemm_f32(ctx, n, n, n, w32, 2 * (long long)n2, n, true, T, 2 * (long long)n2, n, 1.f, 0.f,
+                          reinterpret_cast<float*>(C), 2 * (long long)nn, ld, nk, OLC_STAGE_SOLVE)))
+    return st;
+  cudaFreeAsync(T, stream);
+  float2* H = C;
+  float2* Xc = Zc;
   // ---- 2. tridiagonalisation ----------------------------------------------
   double *d = nullptr, *e = nullptr, *lam = nullptr, *work = nullptr, *Z = nullptr;
   float2* tau = nullptr;
@@ -810,32 +947,39 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&e, 8ULL * (n - 1) * nk, stream), "malloc e"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 1);
-    const size_t smem = 4 * sizeof(float2) * (size_t)ld;
-    if ((st = cuda_check(cudaFuncSetAttribute(hetrd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem), "hetrd smem"))) return st;
+    StageScope scope(ctx, OLC_STAGE_TRIDIAG, 1);
+    // streamed traffic: the trailing lower triangle read and written at every step
+    add_work(ctx, OLC_STAGE_TRIDIAG, 0.0, 8.0 * ((double)n * n * n - n) / 3.0 * nk);
+    const bool det = hetrd_det(ld);
+    const size_t smem = hetrd_smem(ld, det);
+    if ((st = cuda_check(cudaFuncSetAttribute(det ? hetrd_kernel<true> : hetrd_kernel<false>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "hetrd smem"))) return st;
+    if ((st = cuda_check(cudaFuncSetAttribute(det ? hetrd_kernel<true> : hetrd_kernel<false>,
+                                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                         "hetrd cluster size"))) return st;
     int G = 0;
     if (const char* v = std::getenv("OLC_TRD_CLUSTER")) {
       const int g = std::atoi(v);
-      if (g == 1 || g == 2 || g == 4 || g == 8) G = g;
+      if (g == 1 || g == 2 || g == 4 || g == 8 || g == 16) G = g;
     }
     if (!G && (st = tune_cluster(ctx, H, n, ld, nk, smem, d, e, tau, &G))) return st;
     if ((st = launch_hetrd(ctx, G, H, n, ld, nk, smem, d, e, tau))) return st;
   }
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
-  const size_t T = (size_t)n * nk;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&lam, 8ULL * T, stream), "malloc lam"))) return st;
+  const size_t TT = (size_t)n * nk;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&lam, 8ULL * TT, stream), "malloc lam"))) return st;
   float *df = nullptr, *ef = nullptr;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&df, 4ULL * T, stream), "malloc df"))) return st;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&ef, 4ULL * T, stream), "malloc ef"))) return st;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&work, 8ULL * 5 * n * T, stream), "malloc invit work"))) return st;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&piv, (size_t)n * T, stream), "malloc piv"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&df, 4ULL * TT, stream), "malloc df"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&ef, 4ULL * TT, stream), "malloc ef"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&work, 8ULL * 5 * n * TT, stream), "malloc invit work"))) return st;
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&piv, (size_t)n * TT, stream), "malloc piv"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&Z, 8ULL * n * n * nk, stream), "malloc Z"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 3);
-    tri_prep_kernel<<<(int)((T + 255) / 256), 256, 0, stream>>>(d, e, n, nk, df, ef);
-    bisect_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(df, ef, n, nk, lam);
-    invit_kernel<<<(int)((T + 127) / 128), 128, 0, stream>>>(d, e, lam, n, nk, work, piv, Z);
+    StageScope scope(ctx, OLC_STAGE_SOLVE, 4);
+    tri_prep_kernel<<<(int)((TT + 255) / 256), 256, 0, stream>>>(d, e, n, nk, df, ef);
+    bisect_kernel<<<(int)((TT + 127) / 128), 128, 0, stream>>>(df, ef, n, nk, lam);
+    invit_kernel<<<(int)((TT + 127) / 128), 128, 0, stream>>>(d, e, lam, n, nk, work, piv, Z);
     const size_t gsm = sizeof(int) * 2 * (size_t)(n / 2 + 1);
     if ((st = cuda_check(cudaFuncSetAttribute(group_mgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)gsm), "mgs smem"))) return st;
@@ -845,10 +989,9 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
   cudaFreeAsync(piv, stream);
   cudaFreeAsync(df, stream);
   cudaFreeAsync(ef, stream);
-  // ---- 4. back-transform X = Q Z_T ------------------------------------------
+  // ---- 4. back-transform Z = Q Z_T ------------------------------------------
   {
     const int nblk = (n - 1 + kWyBlock - 1) / kWyBlock;
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
     float2 *V = nullptr, *Gm = nullptr, *Tm = nullptr, *W1 = nullptr, *W2 = nullptr;
     const size_t nb = kWyBlock;
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&V, 8ULL * nb * n * nk, stream), "malloc V"))) return st;
@@ -856,34 +999,36 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&Tm, 8ULL * nb * nb * nk, stream), "malloc T"))) return st;
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&W1, 8ULL * nb * n * nk, stream), "malloc W1"))) return st;
     if ((st = cuda_check(ctx_malloc(ctx, (void**)&W2, 8ULL * nb * n * nk, stream), "malloc W2"))) return st;
-    auto* Vc = reinterpret_cast<cuComplex*>(V);
-    auto* Gc = reinterpret_cast<cuComplex*>(Gm);
-    auto* Tc = reinterpret_cast<cuComplex*>(Tm);
-    auto* W1c = reinterpret_cast<cuComplex*>(W1);
-    auto* W2c = reinterpret_cast<cuComplex*>(W2);
-    auto* Zx = reinterpret_cast<cuComplex*>(Xc);
-    // thin FP32 products (K = 128): plain FP32 GEMMs are faster here than the
-    // BF16x9 emulation the Loewdin products use
+    float* Vf = reinterpret_cast<float*>(V);
+    float* Zf = reinterpret_cast<float*>(Xc);
     for (int b = nblk - 1; b >= 0; --b) {
       const int j0 = b * kWyBlock;
       const int nbb = std::min(kWyBlock, n - 1 - j0);
       const int L = n - j0;
-      const long long sV = (long long)nbb * L, sG = (long long)nbb * nbb, sW = (long long)nbb * n;
-      build_v_kernel<<<std::min<size_t>((sV * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(H, n, ld, j0, nbb, L, nk, V);
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nbb, nbb, L, &one, Vc, L, sV, Vc, L, sV,
-                                    &zero, Gc, nbb, sG, nk) != CUBLAS_STATUS_SUCCESS)
-        return fail(OLC_ERR_CUDA, "cgemm V^H V failed");
-      tfactor_kernel<<<nk, kWyBlock, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_C, CUBLAS_OP_N, nbb, n, L, &one, Vc, L, sV,
-                                    Zx + j0, ld, (long long)nn, &zero, W1c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
-        return fail(OLC_ERR_CUDA, "cgemm V^H Z failed");
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, nbb, n, nbb, &one, Tc, nbb, sG,
-                                    W1c, nbb, sW, &zero, W2c, nbb, sW, nk) != CUBLAS_STATUS_SUCCESS)
-        return fail(OLC_ERR_CUDA, "cgemm T W failed");
-      if (cublasCgemmStridedBatched(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, L, n, nbb, &mone, Vc, L, sV,
-                                    W2c, nbb, sW, &one, Zx + j0, ld, (long long)nn, nk) != CUBLAS_STATUS_SUCCESS)
-        return fail(OLC_ERR_CUDA, "cgemm Z -= V W failed");
-      scope.add_launches(2);
+      const long long sV = 2LL * nbb * L, sG = 2LL * nbb * nbb, sW = 2LL * nbb * n;
+      {
+        StageScope scope(ctx, OLC_STAGE_BACKTRANSFORM, 1);
+        build_v_kernel<<<std::min<size_t>((size_t)nbb * L * nk / 256 + 1, 152 * 16), 256, 0, stream>>>(
+            H, n, ld, j0, nbb, L, nk, V);
+      }
+      // G = V^H V, T (clarft), W1 = V^H Z, W2 = T W1, Z -= V W2
+      if ((st = tc::cgemm_f32(ctx, nbb, nbb, L, Vf, sV, L, true, Vf, sV, L, 1.f, 0.f,
+                              reinterpret_cast<float*>(Gm), sG, nbb, nk, OLC_STAGE_BACKTRANSFORM)))
+        return st;
+      {
+        StageScope scope(ctx, OLC_STAGE_BACKTRANSFORM, 1);
+        tfactor_kernel<<<nk, kWyBlock, 0, stream>>>(Gm, tau, n, j0, nbb, Tm);
+      }
+      if ((st = tc::cgemm_f32(ctx, nbb, n, L, Vf, sV, L, true, Zf + 2 * j0, 2 * (long long)nn, ld, 1.f, 0.f,
+                              reinterpret_cast<float*>(W1), sW, nbb, nk, OLC_STAGE_BACKTRANSFORM)))
+        return st;
+      if ((st = tc::cgemm_f32(ctx, nbb, n, nbb, reinterpret_cast<float*>(Tm), sG, nbb, false,
+                              reinterpret_cast<float*>(W1), sW, nbb, 1.f, 0.f, reinterpret_cast<float*>(W2), sW, nbb,
+                              nk, OLC_STAGE_BACKTRANSFORM)))
+        return st;
+      if ((st = tc::cgemm_f32(ctx, L, n, nbb, Vf, sV, L, false, reinterpret_cast<float*>(W2), sW, nbb, -1.f, 1.f,
+                              Zf + 2 * j0, 2 * (long long)nn, ld, nk, OLC_STAGE_BACKTRANSFORM)))
+        return st;
     }
     cudaFreeAsync(V, stream);
     cudaFreeAsync(Gm, stream);
@@ -891,27 +1036,17 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, float* h32, float* s32, 
     cudaFreeAsync(W1, stream);
     cudaFreeAsync(W2, stream);
   }
-  // ---- 5. X = U^{-1} Z --------------------------------------------------------
-  {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
-    if (cublasCtrsmBatched(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, Sp, ld, Xp, ld, nk) != CUBLAS_STATUS_SUCCESS)
-      return fail(OLC_ERR_CUDA, "ctrsmBatched (U^-1 Z) failed");
-  }
-  if (ld != n) {
-    relayout_kernel<<<(int)std::min<size_t>((nn * nk + 255) / 256, 152 * 16), 256, 0, stream>>>(
-        Xc, n, ld, n, nk, reinterpret_cast<float2*>(X));
-    count_launch();
-    cudaFreeAsync(H, stream);
-    cudaFreeAsync(Sq_alloc, stream);
-    cudaFreeAsync(Xc, stream);
-  }
+  // ---- 5. X = W Z ---------------------------------------------------------------
+  if ((st = tc::cgemm_f32(ctx, n, n, n, w32, 2 * (long long)n2, n, false, reinterpret_cast<float*>(Xc),
+                          2 * (long long)nn, ld, 1.f, 0.f, X, 2 * (long long)n2, n, nk, OLC_STAGE_BACKTRANSFORM)))
+    return st;
+  cudaFreeAsync(C, stream);
+  cudaFreeAsync(Zc, stream);
   cudaFreeAsync(d, stream);
   cudaFreeAsync(e, stream);
   cudaFreeAsync(tau, stream);
   cudaFreeAsync(lam, stream);
   cudaFreeAsync(Z, stream);
-  cudaFreeAsync(ptrs, stream);
   return cuda_check(cudaGetLastError(), "batched FP32 solve");
 }
 

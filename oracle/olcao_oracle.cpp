@@ -451,6 +451,9 @@ struct Oracle {
   }
 
   std::string err;
+  // optional subset of atom pairs (i <= j) the operator passes visit; empty:
+  // all pairs.  Lets large systems be checked block by block.
+  std::vector<char> pairMask;
 
   int setup(const olc_system_t* s) {
     for (int i = 0; i < 3; ++i)
@@ -706,6 +709,7 @@ struct Oracle {
 #pragma omp for schedule(dynamic, 1)
     for (long pi = 0; pi < (long)pairList.size(); ++pi) {
       const int i = pairList[pi].first, j = pairList[pi].second;
+      if (!pairMask.empty() && !pairMask[(size_t)i * nsites + j]) continue;
       const TypeInfo& t1 = types[siteType[i]];
       const double* A = &sitePos[3 * i];
       {
@@ -954,6 +958,19 @@ int orc_operator(void* h, int op, int term, double* vv, double* cv, double* cc) 
                            reinterpret_cast<cplx*>(cc));
   if (st) g_err = o->err;
   return st;
+}
+
+// Restricts the operator passes to the listed atom pairs ij[2 * p], ij[2 * p + 1]
+// (0-based, any order); npairs = 0 restores all pairs.
+void orc_set_pairs(void* h, int npairs, const int32_t* ij) {
+  Oracle* o = static_cast<Oracle*>(h);
+  o->pairMask.clear();
+  if (npairs <= 0) return;
+  o->pairMask.assign((size_t)o->nsites * o->nsites, 0);
+  for (int p = 0; p < npairs; ++p) {
+    const int a = std::min(ij[2 * p], ij[2 * p + 1]), b = std::max(ij[2 * p], ij[2 * p + 1]);
+    if (a >= 0 && b < o->nsites) o->pairMask[(size_t)a * o->nsites + b] = 1;
+  }
 }
 
 void orc_ortho_pack(void* h, int is_overlap, double* vv, const double* cv, const double* cc,

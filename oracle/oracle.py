@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
                                    C.c_void_p, C.c_void_p]
         L.orc_operator.restype = C.c_int
         L.orc_ortho_pack.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 5
+        L.orc_set_pairs.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.orc_primitive.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_boys.argtypes = [C.c_double, C.c_void_p]
         _LIB = L
@@ -117,6 +118,15 @@ class Oracle:
             raise RuntimeError(f"oracle status {st}: {lib().orc_error().decode()}")
         return vv, cv, cc
 
+    def set_pairs(self, pairs=None):
+        """Restrict the operator passes to the atom pairs (i, j) listed
+        (0-based); None restores all pairs.  Blocks of other pairs stay zero."""
+        if not pairs:
+            lib().orc_set_pairs(self.h, 0, None)
+            return
+        ij = np.ascontiguousarray(np.asarray(pairs, np.int32).reshape(-1, 2))
+        lib().orc_set_pairs(self.h, int(ij.shape[0]), _p(ij))
+
     def ortho_pack(self, is_overlap: bool, vv, cv, cc, scv) -> np.ndarray:
         nv, nk = self.vale_dim, self.nk
         packed = np.zeros((nk, nv * (nv + 1) // 2, 2))
@@ -142,6 +152,57 @@ class Oracle:
             vv, cv, cc = self.operator(OP_ELECPOT, j)
             out[f"V{j}"] = self.ortho_pack(False, vv, cv, cc, cvS)
         return out
+
+
+def state_offsets(system):
+    """First valence and core state of every atom: the valence-first
+    numbering of cumulValeStates / cumulCoreStates (atomicSites.f90:132-137)."""
+    nv = np.array([system.types[t].num_vale_states for t in system.site_type])
+    nc = np.array([system.types[t].num_core_states for t in system.site_type])
+    cv = np.concatenate([[0], np.cumsum(nv)])
+    cc = np.concatenate([[0], np.cumsum(nc)])
+    return cv, cc
+
+
+def ortho_pack_blas(is_overlap: bool, vv, cv, cc, scv) -> np.ndarray:
+    """orthoOL / ortho(opCode) of integrals.F90:2601-2853 with intgOrtho.F90:23-187
+    restated with matrix products (the reference itself calls zherk/zher2k
+    for the first term):
+
+        O' = O_vv - (S_cv^H O_cv + O_cv^H S_cv) + S_cv^H O_cc S_cv
+        S' = S_vv - 2 S_cv^H S_cv               + S_cv^H S_cc S_cv
+
+    upper triangle, the diagonal of the first update made real (zherk /
+    zher2k), packed column by column, |re|, |im| < 1e-10 flushed to zero when
+    there are core states (intgOrtho.F90:178-183).  Array shapes as
+    Oracle.operator returns them ([nk, cols, rows] memory order); the same
+    numbers as Oracle.ortho_pack up to the order of the sums, fast enough for
+    the largest workloads."""
+    nk, nv = vv.shape[0], vv.shape[1]
+    rows, cols = packed_index(nv)
+    out = np.zeros((nk, nv * (nv + 1) // 2, 2))
+    for q in range(nk):
+        V = vv[q].T
+        if cv is None or cv.shape[2] == 0:
+            vals = V[rows, cols]
+            out[q, :, 0], out[q, :, 1] = vals.real, vals.imag
+            continue
+        Sm = scv[q].T                       # [nc, nv]
+        Om = cv[q].T
+        if is_overlap:
+            T1 = -2.0 * (Sm.conj().T @ Sm)
+        else:
+            T1 = -(Sm.conj().T @ Om + Om.conj().T @ Sm)
+        W = V + T1
+        d = np.arange(nv)
+        W[d, d] = V[d, d].real + T1[d, d].real
+        W = W + (Sm.conj().T @ cc[q].T) @ Sm
+        vals = W[rows, cols]
+        re, im = vals.real.copy(), vals.imag.copy()
+        re[np.abs(re) < 1.0e-10] = 0.0
+        im[np.abs(im) < 1.0e-10] = 0.0
+        out[q, :, 0], out[q, :, 1] = re, im
+    return out
 
 
 def assemble(packed: Dict[str, np.ndarray], coeffs: np.ndarray) -> np.ndarray:

@@ -18,7 +18,7 @@ BAND_TOL = 1e-5
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("m,n,k", [(40, 33, 17), (64, 64, 300), (31, 90, 1500)])
+@pytest.mark.parametrize("m,n,k", [(40, 33, 17), (64, 64, 300), (31, 90, 1500), (200, 260, 2100)])
 def test_split_zgemm_is_fp64_accurate(gpu_lib, m, n, k):
     import torch
     from olcao_gb300 import api
@@ -33,6 +33,29 @@ def test_split_zgemm_is_fp64_accurate(gpu_lib, m, n, k):
     # error bounded by FP64 rounding of |A||B| (per row/column scale)
     bound = 4 * k * 2.0 ** -52 * (np.abs(A) @ np.abs(B))
     assert (np.abs(C - ref) <= bound + 1e-300).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,n,k,conj", [(40, 33, 17, False), (130, 300, 257, True),
+                                        (257, 129, 1000, False), (832, 832, 832, True)])
+def test_split_cgemm32_is_fp32_accurate(gpu_lib, m, n, k, conj):
+    """Tensor-core product from three BF16 pieces per FP32 operand: within
+    FP32 rounding of |op(A)| |B| (element by element)."""
+    import torch
+    from olcao_gb300 import api
+    rng = np.random.default_rng(m * 7 + n + k)
+    shape_a = (k, m) if conj else (m, k)
+    A = (rng.standard_normal(shape_a) + 1j * rng.standard_normal(shape_a)).astype(np.complex64)
+    A *= np.exp(rng.uniform(-3, 3, (shape_a[0], 1))).astype(np.float32)
+    B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))).astype(np.complex64)
+    ctx = api.Context(S.small_test_system("tiny", nk=(1, 1, 1)))
+    C = ctx.split_cgemm32(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), conj_a=conj).cpu().numpy()
+    Ad = A.astype(np.complex128)
+    opA = Ad.conj().T if conj else Ad
+    ref = opA @ B.astype(np.complex128)
+    # three pieces keep 24 bits; FP32 accumulation adds ~sqrt(K) roundings
+    bound = (8 + 2 * np.sqrt(2 * k)) * 2.0 ** -24 * (np.abs(opA) @ np.abs(B.astype(np.complex128))) + 1e-30
+    assert (np.abs(C - ref) <= bound).all(), float((np.abs(C - ref) / bound).max())
 
 
 def _band_energy(w, nocc):
