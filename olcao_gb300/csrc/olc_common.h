@@ -283,10 +283,12 @@ int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num
 // C[b] = op(A[b]) B[b], A logical m x k (conjA: A = src^H), B k x n, C m x n
 // complex FP64 with batch stride m*n; bits_a/bits_b = bits kept per operand;
 // batch strides sA, sB count elements of TA / TB (two per complex number).
+// hermitian: the product is known to be Hermitian (only its upper part is
+// formed, the lower filled by symmetry).
 template <class TA, class TB>
 int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
-                int nb, int stage = OLC_STAGE_REFINE);
+                int nb, int stage = OLC_STAGE_REFINE, bool hermitian = false);
 void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
 
 // status of a queued mixed solve (olc_mixed.cu)

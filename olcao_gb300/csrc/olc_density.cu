@@ -323,7 +323,8 @@ int make_valence_rho(olc_context* ctx, int num_states, int spin, const double* o
           df + (size_t)s * nk * nocc, A, B);
     }
     if ((rc = ozaki_zgemm<double, double>(ctx, n, n, nocc, A, 2LL * n * nocc, n, false, 53, B, 2LL * nocc * n,
-                                          nocc, 53, rho + 2 * (size_t)s * nn * nk, nk, OLC_STAGE_DENSITY)))
+                                          nocc, 53, rho + 2 * (size_t)s * nn * nk, nk, OLC_STAGE_DENSITY,
+                                          true)))
       return rc;
   }
   double* rho1 = rho + 2 * nn * nk;

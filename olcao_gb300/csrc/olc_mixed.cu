@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(1024) cluster_sort_kernel(const double* __rest
 constexpr double kCoupleRatio = 1e-2;
 constexpr double kCoupleFloor = 1e-9;
 __global__ void __launch_bounds__(256) coupling_reach_kernel(const double* __restrict__ Hh, int n, int nk,
-                                                             ClusterLists L, int* __restrict__ reach) {
+                                                             ClusterLists L, double ratio,
+                                                             int* __restrict__ reach) {
   const int gw = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (gw >= n * nk) return;
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(256) coupling_reach_kernel(const double* __res
     const double ar = col[2 * j], ai = col[2 * j + 1];
     const double a2 = ar * ar + ai * ai;
     const double dlt = fabs(ap - diag[j]);
-    if (a2 > kCoupleFloor * kCoupleFloor && a2 > kCoupleRatio * kCoupleRatio * dlt * dlt) far = max(far, pj);
+    if (a2 > kCoupleFloor * kCoupleFloor && a2 > ratio * ratio * dlt * dlt) far = max(far, pj);
   }
   for (int o = 16; o; o >>= 1) far = max(far, __shfl_xor_sync(0xffffffffu, far, o));
   if (lane == 0 && far >= 0) atomicMax(&reach[(size_t)k * n + pp], far);
@@ -834,12 +835,12 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, h, snn, n, false, b64, X, snn, n, b32, Y, nk,
                                        OLC_STAGE_SPLIT))) return st;
   if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Hh, nk,
-                                       OLC_STAGE_SPLIT))) return st;
+                                       OLC_STAGE_SPLIT, true))) return st;
   // Y = S X ; Sh = X^H Y
   if ((st = ozaki_zgemm<double, float>(ctx, n, n, n, s, snn, n, false, b64, X, snn, n, b32, Y, nk,
                                        OLC_STAGE_SPLIT))) return st;
   if ((st = ozaki_zgemm<float, double>(ctx, n, n, n, X, snn, n, true, b32, Y, snn, n, b64, Sh, nk,
-                                       OLC_STAGE_SPLIT))) return st;
+                                       OLC_STAGE_SPLIT, true))) return st;
   cudaFreeAsync(Y, stream);
   // ---- 3. Loewdin transform: Sh = I + E  ->  (I+F)^H Hh (I+F), F = -E/2 + 3E^2/8
   // so that the pencil is standard; the products with the small F need only
@@ -861,7 +862,7 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&reach, 4ULL * n * nk, stream), "malloc reach"))) return st;
   if (vectors && (st = cuda_check(ctx_malloc(ctx, (void**)&v_slot, 16ULL * nn * nk, stream), "malloc v"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_REFINE, 6);
+    StageScope scope(ctx, OLC_STAGE_REFINE, 5);
     int P = 1;
     while (P < n) P <<= 1;
     const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
@@ -872,7 +873,14 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     if ((st = cuda_check(cudaMemsetAsync(L.counters, 0, 4 * sizeof(int), stream), "memset"))) return st;
     cluster_sort_kernel<<<nk, 1024, sortmem, stream>>>(Hh, n, L);
     if ((st = cuda_check(cudaMemsetAsync(reach, 0xff, 4ULL * n * nk, stream), "memset reach"))) return st;
-    coupling_reach_kernel<<<(int)(((size_t)n * nk * 32 + 255) / 256), 256, 0, stream>>>(Hh, n, nk, L, reach);
+    // OLC_COUPLE_RATIO overrides the coupling ratio (0: gaps alone form the clusters)
+    double ratio = kCoupleRatio;
+    if (const char* v = std::getenv("OLC_COUPLE_RATIO")) ratio = std::atof(v);
+    if (ratio > 0.0) {
+      coupling_reach_kernel<<<(int)(((size_t)n * nk * 32 + 255) / 256), 256, 0, stream>>>(Hh, n, nk, L, ratio,
+                                                                                          reach);
+      scope.add_launches(1);
+    }
     const size_t formmem = (size_t)n * (sizeof(double) + sizeof(int));
     if ((st = cuda_check(cudaFuncSetAttribute(cluster_form_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)formmem), "smem attribute"))) return st;

@@ -260,12 +260,13 @@ void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs) {
 template <class TA, class TB>
 int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
-                int nb, int stage) {
+                int nb, int stage, bool hermitian) {
   // the hand-written tcgen05 kernel (olc_tcgemm.cu) unless OLC_SPLIT_GEMM=cublas
   // selects the library GEMM path below
   const char* path = std::getenv("OLC_SPLIT_GEMM");
   if (!(path && std::strcmp(path, "cublas") == 0))
-    return tc::zgemm_fixed<TA, TB>(ctx, m, n, k, A, sA, lda, conjA, bits_a, B, sB, ldb, bits_b, C, nb, stage);
+    return tc::zgemm_fixed<TA, TB>(ctx, m, n, k, A, sA, lda, conjA, bits_a, B, sB, ldb, bits_b, C, nb, stage,
+                                   hermitian);
   cudaStream_t st = ctx->stream;
   int beta, na, nbs;
   ozaki_plan(k, bits_a, bits_b, &beta, &na, &nbs);
@@ -333,10 +334,10 @@ int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
 }
 
 template int ozaki_zgemm<double, float>(olc_context*, int, int, int, const double*, long long, int, bool,
-                                        int, const float*, long long, int, int, double*, int, int);
+                                        int, const float*, long long, int, int, double*, int, int, bool);
 template int ozaki_zgemm<float, double>(olc_context*, int, int, int, const float*, long long, int, bool,
-                                        int, const double*, long long, int, int, double*, int, int);
+                                        int, const double*, long long, int, int, double*, int, int, bool);
 template int ozaki_zgemm<double, double>(olc_context*, int, int, int, const double*, long long, int, bool,
-                                         int, const double*, long long, int, int, double*, int, int);
+                                         int, const double*, long long, int, int, double*, int, int, bool);
 
 }  // namespace olc

@@ -216,6 +216,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   int mt, nt;
   tile_of(blockIdx.x, p.nmt, p.nnt, mt, nt);
   const int m0 = mt * BM, n0 = nt * BN;     // n0: first real column of D
+  // Hermitian result: a tile whose complex columns all lie left of its first
+  // row is wholly below the diagonal (filled afterwards from the upper part)
+  if (p.herm_upper && (n0 >> 1) + BN / 2 - 1 < m0) return;
   // segments: every pair over K chunks of chunk_blocks K-blocks
   const int nchunk = (p.kblocks + p.chunk_blocks - 1) / p.chunk_blocks;
   const int nseg = p.npairs * nchunk;
@@ -339,9 +342,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             for (int j = 0; j < 16; ++j)
               acc[16 * part + j] += (long long)__float2int_rn(__uint_as_float(r[j])) << sh;
           } else {
+            // low-order digit groups: rounded to the accumulator's unit (a
+            // plain arithmetic shift would floor, a bias of half a unit per
+            // drain that adds up over long K)
+            const long long half = 1LL << (-sh - 1);
 #pragma unroll
             for (int j = 0; j < 16; ++j)
-              acc[16 * part + j] += (long long)__float2int_rn(__uint_as_float(r[j])) >> (-sh);
+              acc[16 * part + j] += ((long long)__float2int_rn(__uint_as_float(r[j])) + half) >> (-sh);
           }
         }
       }
@@ -567,6 +574,30 @@ __global__ void slice_b_kernel(const T* __restrict__ src, long long sstride, int
 
 int grid_of(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
+// C(r, c) = conj(C(c, r)) for r > c: the strict lower triangle of a
+// Hermitian batch [nb][n][n] (complex FP64, column-major) from its upper one.
+__global__ void mirror_lower_kernel(double2* __restrict__ C, int n, int nb) {
+  __shared__ double2 tile[32][33];
+  const int b = blockIdx.z;
+  const int bx = blockIdx.x, by = blockIdx.y;   // tile (rows by, columns bx) of the lower part
+  if (bx > by) return;
+  double2* Cb = C + (size_t)b * n * n;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  // read the upper tile (rows bx, columns by), write its conjugate transpose
+  for (int j = ty; j < 32; j += 8) {
+    const int r = bx * 32 + tx, c = by * 32 + j;
+    if (r < n && c < n) tile[j][tx] = Cb[(size_t)c * n + r];
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int r = by * 32 + tx, c = bx * 32 + j;     // lower element (r, c) = conj(upper (c, r))
+    if (r < n && c < n && r > c) {
+      const double2 u = tile[tx][j];
+      Cb[(size_t)c * n + r] = make_double2(u.x, -u.y);
+    }
+  }
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against libcuda).
 using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -644,7 +675,14 @@ int launch(olc_context* ctx, int mode, const void* dA, const void* dB, int plane
     tc_gemm_kernel<1><<<grid, NUM_THREADS, smem, st>>>(ta, tb, p);
   }
   count_launch();
-  add_work(ctx, stage, 2.0 * m * (double)nreal * (double)Kp * p.npairs * nb, 0.0);
+  double frac = 1.0;
+  if (p.herm_upper) {
+    long long done = 0;
+    for (int mt = 0; mt < p.nmt; ++mt)
+      for (int nt = 0; nt < p.nnt; ++nt) done += ((nt * BN) / 2 + BN / 2 - 1 >= mt * BM);
+    frac = (double)done / ((double)p.nmt * p.nnt);
+  }
+  add_work(ctx, stage, 2.0 * m * (double)nreal * (double)Kp * p.npairs * nb * frac, 0.0);
   return cuda_check(cudaGetLastError(), "tc_gemm launch");
 }
 
@@ -672,7 +710,8 @@ int read_error(int* code) {
 
 template <class TA, class TB>
 int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda, bool conjA, int bits_a,
-                const TB* B, long long sB, int ldb, int bits_b, double* C, int nb, int stage) {
+                const TB* B, long long sB, int ldb, int bits_b, double* C, int nb, int stage, bool hermitian) {
+  if (hermitian && m != n) return fail(OLC_ERR_ARG, "hermitian product must be square");
   cudaStream_t st = ctx->stream;
   int na, nbd, T;
   // the product is wanted to the precision of the wider operand (the
@@ -731,7 +770,13 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
     p.npairs = (int)pairs.size();
     for (size_t i = 0; i < pairs.size(); ++i) p.pairs[i] = pairs[i];
     p.chunk_blocks = 1024 / BK;
+    p.herm_upper = hermitian ? 1 : 0;
     if ((s = launch(ctx, 0, wa, wb, na, nbd, Kp, m, 2 * n, cb, p, stage))) return s;
+    if (hermitian) {
+      StageScope ms(ctx, stage, 1);
+      mirror_lower_kernel<<<dim3((n + 31) / 32, (n + 31) / 32, cb), dim3(32, 8), 0, st>>>(
+          reinterpret_cast<double2*>(C + 2 * (size_t)b0 * m * n), n, cb);
+    }
   }
   cudaFreeAsync(wa, st);
   cudaFreeAsync(wb, st);
@@ -784,11 +829,11 @@ int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long s
 }
 
 template int zgemm_fixed<double, float>(olc_context*, int, int, int, const double*, long long, int, bool, int,
-                                        const float*, long long, int, int, double*, int, int);
+                                        const float*, long long, int, int, double*, int, int, bool);
 template int zgemm_fixed<float, double>(olc_context*, int, int, int, const float*, long long, int, bool, int,
-                                        const double*, long long, int, int, double*, int, int);
+                                        const double*, long long, int, int, double*, int, int, bool);
 template int zgemm_fixed<double, double>(olc_context*, int, int, int, const double*, long long, int, bool, int,
-                                         const double*, long long, int, int, double*, int, int);
+                                         const double*, long long, int, int, double*, int, int, bool);
 
 }  // namespace tc
 }  // namespace olc

@@ -32,15 +32,20 @@ struct TcParams {
   int planes_a, planes_b;       // planes per batch entry
   int nmt, nnt;                 // tiles
   int npairs, kblocks, chunk_blocks;   // segments: pairs x ceil(kblocks / chunk_blocks) K chunks
+  int herm_upper;               // Hermitian result: tiles wholly below the diagonal are skipped
   int* err;                     // device error word (expired waits)
   TcPair pairs[kMaxPairs];
 };
 
 // FP64-accurate complex product C[b] = op(A[b]) B[b] (m x n, column-major,
 // ld m) from 7-bit digit planes: bits_a / bits_b bits kept of A / B.
+// hermitian: the result is known to be Hermitian (m == n); only the tiles
+// that touch the upper triangle are computed and the strict lower triangle
+// is filled from it.
 template <class TA, class TB>
 int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda, bool conjA, int bits_a,
-                const TB* B, long long sB, int ldb, int bits_b, double* C, int nb, int stage);
+                const TB* B, long long sB, int ldb, int bits_b, double* C, int nb, int stage,
+                bool hermitian = false);
 
 // FP32-accurate complex product C[b] = alpha op(A[b]) B[b] + beta C[b] from
 // three BF16 pieces per FP32 operand (six piece pairs).
