@@ -288,6 +288,9 @@ int64_t olc_launch_count(void);
  *
  * The first call on a device looks up that array's device address (with
  * the device current); make that first call before any stream capture.
+ * The address is kept per device ordinal for the life of the process: it
+ * is not valid after cudaDeviceReset, nor under a second, non-primary
+ * context on the same device.
  * Work is queued on `stream` (NULL = legacy stream) and not synchronised.
  * Calls share the array and every call overwrites all of the part it uses,
  * so nothing is carried over between calls, but calls that overlap on the

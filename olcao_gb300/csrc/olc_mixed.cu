@@ -159,7 +159,8 @@ __global__ void __launch_bounds__(256) coupling_reach_kernel(const double* __res
 // each cut side (only its own eigenpairs are kept), so that the strongly
 // coupled states across a cut are treated exactly.  Appends every cluster
 // except clean single states to a work list.
-__global__ void __launch_bounds__(256) cluster_form_kernel(int n, ClusterLists L, const int* __restrict__ reach) {
+__global__ void __launch_bounds__(256) cluster_form_kernel(int n, ClusterLists L, const int* __restrict__ reach,
+                                                           double gap) {
   extern __shared__ double formmem[];
   double* keys = formmem;
   int* rk = reinterpret_cast<int*>(formmem + n);
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(256) cluster_form_kernel(int n, ClusterLists L
   };
   int s0 = 0, span = rk[0];
   for (int i = 1; i <= n; ++i) {
-    if (i < n && (key(i) - key(i - 1) < kClusterGap || span >= i)) {
+    if (i < n && (key(i) - key(i - 1) < gap || span >= i)) {
       span = max(span, rk[i]);
       continue;
     }
@@ -884,7 +885,10 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     const size_t formmem = (size_t)n * (sizeof(double) + sizeof(int));
     if ((st = cuda_check(cudaFuncSetAttribute(cluster_form_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)formmem), "smem attribute"))) return st;
-    cluster_form_kernel<<<nk, 256, formmem, stream>>>(n, L, reach);
+    // OLC_CLUSTER_GAP overrides the gap that separates clusters (Hartree)
+    double gap = kClusterGap;
+    if (const char* v = std::getenv("OLC_CLUSTER_GAP")) gap = std::atof(v);
+    cluster_form_kernel<<<nk, 256, formmem, stream>>>(n, L, reach, gap);
     singleton_kernel<<<(int)(((size_t)n * nk * 32 + 255) / 256), 256, 0, stream>>>(Hh, X, L, n, nk, w_slot,
                                                                                   v_slot);
     const size_t sm_small = sizeof(ClusterSmem<kSmallCluster>), sm_large = sizeof(ClusterSmem<kMaxCluster>);

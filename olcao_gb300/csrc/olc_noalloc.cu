@@ -9,6 +9,7 @@
 // libraries call cudaMalloc/cudaFree.  They pass device pointers for every
 // input and output; this call allocates nothing.
 #include <mutex>
+#include <string>
 
 #include "olc_common.h"
 
@@ -83,13 +84,16 @@ extern "C" int olc_solve_zhegv_noalloc(int n, int nk, const double* packed_h,
     return fail(OLC_ERR_ARG, "olc_solve_zhegv_noalloc: null or empty argument");
   if (num_states < 1 || num_states > n)
     return fail(OLC_ERR_ARG, "olc_solve_zhegv_noalloc: num_states out of range");
-  if (n > small_solver_capacity_n())
-    return fail(OLC_ERR_ARG, "olc_solve_zhegv_noalloc: n exceeds 64, the largest size this "
-                             "allocation-free solver handles");
+  const int nmax = small_solver_capacity_n();
+  if (n > nmax)
+    return fail(OLC_ERR_ARG, "olc_solve_zhegv_noalloc: n exceeds " + std::to_string(nmax) +
+                                 ", the largest size this allocation-free solver handles");
   const size_t need = (size_t)4 * n * n * nk;   // H and S, complex128
   if (need > kScratchDoubles)
-    return fail(OLC_ERR_ARG, "olc_solve_zhegv_noalloc: nk * n * n exceeds 524288, the capacity "
-                             "of its 16 MiB working array; split the k-points into batches");
+    return fail(OLC_ERR_ARG, "olc_solve_zhegv_noalloc: nk * n * n exceeds " +
+                                 std::to_string(kScratchDoubles / 4) + ", the capacity of its " +
+                                 std::to_string(kScratchDoubles * 8 >> 20) +
+                                 " MiB working array; split the k-points into batches");
   double* scratch = nullptr;
   int st = scratch_for_current_device(&scratch);
   if (st) return st;

@@ -40,6 +40,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -58,7 +59,9 @@ constexpr int NUM_EPI_WARPS = 8;
 constexpr int NUM_THREADS = (NUM_EPI_WARPS + 2) * 32;
 constexpr int PRODUCER_WARP = NUM_EPI_WARPS;
 constexpr int MMA_WARP = NUM_EPI_WARPS + 1;
-constexpr int TMEM_COLS = 256;
+// two accumulators of BN columns: 256 (fixed mode) or 512 (f32 mode)
+template <int MODE>
+constexpr int tmem_cols() { return MODE == 0 ? 256 : 512; }
 constexpr long long kWaitNs = 2000000000LL;   // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   }
   if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(tmem_cols<MODE>()));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -286,8 +289,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true;
       for (int si = 0; si < nseg && ok; ++si) {
         const int kb0 = (si % nchunk) * p.chunk_blocks, kb1 = min(p.kblocks, kb0 + p.chunk_blocks);
-        const int buf = MODE == 0 ? (si & 1) : 0;
-        if (MODE == 0) {
+        const int buf = si & 1;
+        {
           const uint32_t use = (uint32_t)(si >> 1);
           if (!mbar_wait(&accempty[buf], (use & 1u) ^ 1u, cta_err, p.err, 2)) { ok = false; break; }
           tc_fence_after();
@@ -300,14 +303,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const uint64_t bd = sdesc(smem_u32(sB + stage * SmemLayout::b_bytes<BN>()));
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {
-            const bool first = (kb == kb0 && k == 0) && (MODE == 0 || si == 0);
+            const bool first = kb == kb0 && k == 0;
             // +32 bytes of K per instruction: +2 in the descriptor's address field
             umma(dt, ad + 2 * k, bd + 2 * k, IDESC, first ? 0u : 1u);
           }
           umma_commit(&empty[stage]);
           if (++stage == STAGES) { stage = 0; phase ^= 1u; }
         }
-        if (ok && (MODE == 0 || si == nseg - 1)) umma_commit(&accfull[buf]);
+        if (ok) umma_commit(&accfull[buf]);
       }
     }
   } else {
@@ -367,30 +370,49 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
       }
     } else {
-      if (__all_sync(0xffffffffu, mbar_wait(&accfull[0], 0u, cta_err, p.err, 4))) {
+      // FP32 mode: every segment (one piece pair over at most 512 of K') is
+      // drained into register accumulators with round-to-nearest adds, so
+      // that long sums of like-signed terms are not left to the tensor
+      // core's accumulator alone
+      float acc[128];
+#pragma unroll
+      for (int j = 0; j < 128; ++j) acc[j] = 0.f;
+      bool ok = true;
+      for (int si = 0; si < nseg; ++si) {
+        const int buf = si & 1;
+        const uint32_t use = (uint32_t)(si >> 1);
+        ok = __all_sync(0xffffffffu, mbar_wait(&accfull[buf], use & 1u, cta_err, p.err, 4));
+        if (!ok) break;
         tc_fence_after();
+#pragma unroll
+        for (int part = 0; part < 8; ++part) {
+          uint32_t r[16];
+          tmem_ld16(lane_addr + (uint32_t)(buf * BN + 128 * h + 16 * part), r);
+          tmem_ld_wait();
+          if (part == 7) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&accempty[buf]);
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[16 * part + j] += __uint_as_float(r[j]);
+        }
+      }
+      if (ok && row < p.m) {
         float2* out = reinterpret_cast<float2*>(p.c32) + (size_t)b * p.stride_c;
         const int cbase = (n0 >> 1) + 64 * h;
-#pragma unroll 1
-        for (int part = 0; part < 4; ++part) {
-          uint32_t r[32];
-          tmem_ld32(lane_addr + (uint32_t)(128 * h + 32 * part), r);
-          tmem_ld_wait();
-          if (row < p.m) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int c = cbase + 16 * part + j;
-              if (c < p.ncols) {
-                float2 v = make_float2(p.alpha * __uint_as_float(r[2 * j]), p.alpha * __uint_as_float(r[2 * j + 1]));
-                float2* o = out + (size_t)c * p.ldc + row;
-                if (p.beta != 0.f) {
-                  const float2 old = *o;
-                  v.x += p.beta * old.x;
-                  v.y += p.beta * old.y;
-                }
-                *o = v;
-              }
+        for (int j = 0; j < 64; ++j) {
+          const int c = cbase + j;
+          if (c < p.ncols) {
+            float2 v = make_float2(p.alpha * acc[2 * j], p.alpha * acc[2 * j + 1]);
+            float2* o = out + (size_t)c * p.ldc + row;
+            if (p.beta != 0.f) {
+              const float2 old = *o;
+              v.x += p.beta * old.x;
+              v.y += p.beta * old.y;
             }
+            *o = v;
           }
         }
       }
@@ -400,7 +422,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   if (warp == MMA_WARP) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols<MODE>()));
   }
 }
 
@@ -791,7 +813,11 @@ int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long s
   cudaStream_t st = ctx->stream;
   const int kp = (k + 31) & ~31;
   const size_t Kp = 2 * (size_t)kp;
-  static const int8_t pairs[6][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}, {0, 2}, {2, 0}};
+  // piece pairs by weight: the six down to 2^-16, and with OLC_F32_PAIRS=9 the
+  // three of weight 2^-24 and below as well
+  static const int8_t pairs[9][2] = {{0, 0}, {0, 1}, {1, 0}, {1, 1}, {0, 2}, {2, 0}, {1, 2}, {2, 1}, {2, 2}};
+  int npairs = 6;
+  if (const char* v = std::getenv("OLC_F32_PAIRS")) npairs = std::atoi(v) == 9 ? 9 : 6;
   const size_t per_b = 2 * Kp * 3 * ((size_t)m + 2 * (size_t)n);
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>(nb, (8ULL << 30) / std::max<size_t>(per_b, 1)));
   __nv_bfloat16 *wa = nullptr, *wb = nullptr;
@@ -818,9 +844,9 @@ int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long s
     p.c32 = C + (size_t)b0 * sC;
     p.alpha = alpha;
     p.beta = beta;
-    p.npairs = 6;
-    for (int i = 0; i < 6; ++i) p.pairs[i] = TcPair{pairs[i][0], pairs[i][1], 0};
-    p.chunk_blocks = (int)(Kp / BK);
+    p.npairs = npairs;
+    for (int i = 0; i < npairs; ++i) p.pairs[i] = TcPair{pairs[i][0], pairs[i][1], 0};
+    p.chunk_blocks = 512 / BK;
     if ((s = launch(ctx, 1, wa, wb, 3, 3, Kp, m, 2 * n, cb, p, stage))) return s;
   }
   cudaFreeAsync(wa, st);

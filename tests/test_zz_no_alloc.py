@@ -55,13 +55,39 @@ def test_noalloc_solver_matches_the_allocating_solver_twice(gpu_lib):
         assert st == 0, api.last_error()
         assert (info == 0).all() and (info_ref == 0).all()
         assert np.abs(eig - ref.cpu().numpy()).max() <= EIG_TOL
-        # vectors are S-orthonormal
+        # vectors are S-orthonormal and solve the pencil; eigenvalues also
+        # against LAPACK, which shares no code with either device solver
         import oracle as orc
-        Sp = Sm.cpu().numpy()
+        import scipy.linalg as sl
+        Sp, Hp = Sm.cpu().numpy(), Hs.cpu().numpy()
         for k in range(nk):
-            Sk = orc.unpack(Sp[k], n)
+            Sk, Hk = orc.unpack(Sp[k], n), orc.unpack(Hp[k], n)
             Z = vec[k].T
             assert np.abs(Z.conj().T @ Sk @ Z - np.eye(n)).max() < 1e-9
+            assert np.abs(Hk @ Z - Sk @ Z * eig[k][None, :]).max() < 1e-8 * max(1.0, np.abs(Hk).max())
+            assert np.abs(eig[k] - sl.eigh(Hk, Sk, eigvals_only=True)).max() <= EIG_TOL
+
+
+@pytest.mark.gpu
+def test_noalloc_solver_allocates_no_device_memory(gpu_lib):
+    """After a first call (which looks up the working array's address), more
+    calls leave the free device memory unchanged."""
+    from olcao_gb300 import api
+    ctx, H, Sm, torch = _packed_case()
+    n, nk = ctx.vale_dim, ctx.nk
+    lib = api.lib()
+    eig = torch.zeros(nk, n, dtype=torch.float64, device="cuda")
+    vec = torch.zeros(nk, n, n, dtype=torch.complex128, device="cuda")
+    info = torch.zeros(nk, dtype=torch.int32, device="cuda")
+    args = (n, nk, H.data_ptr(), Sm.data_ptr(), n, eig.data_ptr(), vec.data_ptr(), info.data_ptr(), None)
+    assert lib.olc_solve_zhegv_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        assert lib.olc_solve_zhegv_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
 
 
 @pytest.mark.gpu
@@ -73,7 +99,9 @@ def test_noalloc_solver_refuses_sizes_beyond_its_array(gpu_lib):
     info = torch.zeros(16, dtype=torch.int32, device="cuda")
     st = lib.olc_solve_zhegv_noalloc(65, 1, d.data_ptr(), d.data_ptr(), 1, d.data_ptr(),
                                      None, info.data_ptr(), None)
-    assert st == 1 and "64" in api.last_error()
+    msg = api.last_error()
+    assert st == 1 and "n exceeds 64" in msg
     st = lib.olc_solve_zhegv_noalloc(64, 129, d.data_ptr(), d.data_ptr(), 1, d.data_ptr(),
                                      None, info.data_ptr(), None)
-    assert st == 1 and "524288" in api.last_error()
+    msg = api.last_error()
+    assert st == 1 and "exceeds" in msg and "working array" in msg
