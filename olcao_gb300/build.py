@@ -18,7 +18,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libolcao_gb300.so")
-SOURCES = ["olc_capi.cpp", "olc_setup.cpp", "olc_integrals.cu", "olc_linalg.cu",
+SOURCES = ["olc_capi.cpp", "olc_setup.cpp", "olc_integrals.cu", "olc_integrals_f_overlap.cu",
+           "olc_integrals_f_kinetic.cu", "olc_integrals_f_massvel.cu", "olc_integrals_f_nuclear.cu", "olc_integrals_f_nuclear_batch.cu",
+           "olc_integrals_f_elecpot.cu", "olc_linalg.cu",
            "olc_eigen_small.cu", "olc_noalloc.cu", "olc_mixed.cu", "olc_tridiag.cu",
            "olc_ozaki.cu", "olc_tcgemm.cu", "olc_layout.cu", "olc_density.cu", "olc_populate.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -65,7 +67,7 @@ def build(verbose: bool = False, extra: List[str] = ()) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(16, max(1, len(jobs)))) as ex:
         for cmd, r in ex.map(run, jobs):
             if verbose or r.returncode:
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

@@ -17,8 +17,8 @@
 namespace olc {
 
 constexpr double kPi = 3.141592653589793;
-constexpr int kMaxL = 2;            // highest l the integral kernels are built for
-constexpr int kMaxLm = 9;           // (kMaxL+1)^2 real harmonics s..d
+constexpr int kMaxL = 3;            // highest l the integral kernels are built for
+constexpr int kMaxLm = 16;          // (kMaxL+1)^2 real harmonics s..f
 constexpr int kNumClasses = (kMaxL + 1) * (kMaxL + 1);
 
 // Per-atom-type data the kernels read (basis.f90:55-243 restated).

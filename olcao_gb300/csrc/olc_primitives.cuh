@@ -1,5 +1,5 @@
-// Device Gaussian primitives for l <= 2 per centre (s, p, d Cartesians and
-// the unnormalised real harmonics of gaussIntegrals.f90:33-35).
+// Device Gaussian primitives for l <= 3 per centre (s, p, d, f Cartesians and
+// the unnormalised real harmonics of gaussIntegrals.f90:33-39).
 //
 // All primitives are Obara-Saika recurrences (Obara & Saika, J. Chem. Phys.
 // 84, 3963 (1986)) held in registers, specialised at compile time on the
@@ -20,26 +20,49 @@ namespace olc {
 __host__ __device__ constexpr int ncart(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
 __host__ __device__ constexpr int nharm(int L) { return (L + 1) * (L + 1); }
 
-// Cartesian functions s; x y z; xx yy zz xy xz yz
+// Cartesian functions s; x y z; xx yy zz xy xz yz;
+// xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz
 __host__ __device__ constexpr int cex(int c) {
-  return c == 1 ? 1 : c == 4 ? 2 : c == 7 ? 1 : c == 8 ? 1 : 0;
+  return c == 1 ? 1 : c == 4 ? 2 : c == 7 ? 1 : c == 8 ? 1 : c == 10 ? 3 : c == 13 ? 2 : c == 14 ? 2
+       : c == 15 ? 1 : c == 17 ? 1 : c == 19 ? 1 : 0;
 }
 __host__ __device__ constexpr int cey(int c) {
-  return c == 2 ? 1 : c == 5 ? 2 : c == 7 ? 1 : c == 9 ? 1 : 0;
+  return c == 2 ? 1 : c == 5 ? 2 : c == 7 ? 1 : c == 9 ? 1 : c == 11 ? 3 : c == 13 ? 1 : c == 15 ? 2
+       : c == 16 ? 2 : c == 18 ? 1 : c == 19 ? 1 : 0;
 }
 __host__ __device__ constexpr int cez(int c) {
-  return c == 3 ? 1 : c == 6 ? 2 : c == 8 ? 1 : c == 9 ? 1 : 0;
+  return c == 3 ? 1 : c == 6 ? 2 : c == 8 ? 1 : c == 9 ? 1 : c == 12 ? 3 : c == 14 ? 1 : c == 16 ? 1
+       : c == 17 ? 2 : c == 18 ? 2 : c == 19 ? 1 : 0;
 }
 
-// Real harmonic p (0-based lm) as a combination of Cartesians:
-// s; x y z; xy xz yz; xx-yy; 2zz-xx-yy
-__host__ __device__ constexpr int hn(int p) { return p == 7 ? 2 : p == 8 ? 3 : 1; }
+// Real harmonic p (0-based lm) as a combination of Cartesians (the
+// unnormalised functions of the reference's sh order):
+// s; x y z; xy xz yz; xx-yy; 2zz-xx-yy;
+// xyz; xxz-yyz; xxx-3yyx; 3xxy-yyy; 2zzz-3xxz-3yyz; 4zzx-xxx-yyx; 4zzy-xxy-yyy
+__host__ __device__ constexpr int hn(int p) {
+  return p == 7 ? 2 : p == 8 ? 3 : (p >= 10 && p <= 12) ? 2 : p >= 13 ? 3 : 1;
+}
 __host__ __device__ constexpr int hc(int p, int t) {  // cartesian index of term t
-  return p <= 3 ? p : p == 4 ? 7 : p == 5 ? 8 : p == 6 ? 9 : p == 7 ? (t == 0 ? 4 : 5)
-                                                                     : (t == 0 ? 6 : t == 1 ? 4 : 5);
+  return p <= 3 ? p : p == 4 ? 7 : p == 5 ? 8 : p == 6 ? 9
+       : p == 7 ? (t == 0 ? 4 : 5)
+       : p == 8 ? (t == 0 ? 6 : t == 1 ? 4 : 5)
+       : p == 9 ? 19
+       : p == 10 ? (t == 0 ? 14 : 16)
+       : p == 11 ? (t == 0 ? 10 : 15)
+       : p == 12 ? (t == 0 ? 13 : 11)
+       : p == 13 ? (t == 0 ? 12 : t == 1 ? 14 : 16)
+       : p == 14 ? (t == 0 ? 17 : t == 1 ? 10 : 15)
+       : (t == 0 ? 18 : t == 1 ? 13 : 11);
 }
 __host__ __device__ constexpr double hw(int p, int t) {  // coefficient of term t
-  return p == 7 ? (t == 0 ? 1.0 : -1.0) : p == 8 ? (t == 0 ? 2.0 : -1.0) : 1.0;
+  return p == 7 ? (t == 0 ? 1.0 : -1.0)
+       : p == 8 ? (t == 0 ? 2.0 : -1.0)
+       : p == 10 ? (t == 0 ? 1.0 : -1.0)
+       : p == 11 ? (t == 0 ? 1.0 : -3.0)
+       : p == 12 ? (t == 0 ? 3.0 : -1.0)
+       : p == 13 ? (t == 0 ? 2.0 : -3.0)
+       : (p == 14 || p == 15) ? (t == 0 ? 4.0 : -1.0)
+       : 1.0;
 }
 
 // 1-D Obara-Saika overlap recurrence with unit prefactor:

@@ -170,8 +170,6 @@ int build_system(olc_context* ctx, const olc_system_t* s) {
     for (int l = 1; l < 4; ++l)
       if (at.num_orb_alphas[l] > at.num_orb_alphas[l - 1])
         return fail(OLC_ERR_ARG, "numOrbAlphas must not increase with l");
-    if (at.num_orb_alphas[3] > 0)
-      return fail(OLC_ERR_UNSUPPORTED, "f-type exponents (numOrbAlphas(4) > 0) are not built");
     for (int a = 0; a < d.nalpha; ++a) {
       d.alphas[a] = at.alphas[a];
       if (a > 0 && !(at.alphas[a] > at.alphas[a - 1]))
@@ -183,7 +181,7 @@ int build_system(olc_context* ctx, const olc_system_t* s) {
     if (nrad > OLC_MAX_RADIAL) return fail(OLC_ERR_ARG, "too many radial functions");
     for (int r = 0; r < nrad; ++r) {
       int l = at.radial_l[r];
-      if (l < 0 || l > kMaxL) return fail(OLC_ERR_UNSUPPORTED, "radial l > 2 is not built");
+      if (l < 0 || l > kMaxL) return fail(OLC_ERR_ARG, "radial functions have l = 0..3 (s, p, d, f)");
       int na = at.num_orb_alphas[l];
       for (int k = 1; k <= 2 * l + 1; ++k) {
         if (m >= OLC_MAX_STATES) return fail(OLC_ERR_ARG, "too many states per type");

@@ -362,7 +362,8 @@ def small_test_system(kind: str = "si2", seed: int = 11, nk=(2, 2, 2)) -> System
 
     si2: 2 Si atoms in a small triclinic-ish cell with core states and d
     functions; c2: diamond primitive cell with a coarse mesh; sio: one Si
-    and one O (two types, two potential types)."""
+    and one O (two types, two potential types); sif: sio with f functions
+    on Si (a valence f and a core f), so that every class pair s..f meets."""
     rng = np.random.default_rng(seed)
     if kind == "tiny":
         a = 3.567 * ANGSTROM
@@ -392,6 +393,18 @@ def small_test_system(kind: str = "si2", seed: int = 11, nk=(2, 2, 2)) -> System
                        (0, 1, 0, 1, 2), (0,))
         pots = [silicon_pot(1), PotSpec(2, 8.0, 20.0, even_tempered(16, 0.1, 1.0e6))]
         return _finish("sio", vec, [tsi, to], [0, 1], pos, pots,
+                       mp_mesh(nk, (0.5, 0.5, 0.5)), rng, seed,
+                       pot_of_type={0: 0, 1: 1})
+    if kind == "sif":
+        a = 4.2 * ANGSTROM
+        vec = np.array([[a, 0, 0], [0.1 * a, a, 0], [0.2 * a, 0.1 * a, 1.05 * a]]).T
+        pos = np.array([[0.1, 0.2, 0.3], [1.4, 1.3, 1.8]]) * ANGSTROM
+        tsi = make_type(rng, 1, 18, 0.12, 1.0e6, (18, 18, 12, 8),
+                        (0, 1, 2, 3, 0, 1), (0, 0, 1, 3))
+        to = make_type(rng, 2, 18, 0.12, 1.0e6, (18, 18, 12, 0),
+                       (0, 1, 0, 1, 2), (0,))
+        pots = [silicon_pot(1), PotSpec(2, 8.0, 20.0, even_tempered(16, 0.1, 1.0e6))]
+        return _finish("sif", vec, [tsi, to], [0, 1], pos, pots,
                        mp_mesh(nk, (0.5, 0.5, 0.5)), rng, seed,
                        pot_of_type={0: 0, 1: 1})
     raise ValueError(kind)

@@ -18,7 +18,7 @@ from olcao_gb300 import system as S
 EIG_TOL = 1e-8
 
 
-@pytest.fixture(scope="module", params=["si2", "sio"])
+@pytest.fixture(scope="module", params=["si2", "sio", "sif"])
 def case(request, gpu_lib):
     from olcao_gb300 import api
     sysm = S.small_test_system(request.param, nk=(2, 1, 2))

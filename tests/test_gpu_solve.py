@@ -19,6 +19,7 @@ SYSTEMS = {
     "c2": lambda: S.small_test_system("c2", nk=(2, 2, 2)),
     "si2": lambda: S.small_test_system("si2", nk=(2, 2, 2)),
     "sio": lambda: S.small_test_system("sio", nk=(2, 1, 2)),
+    "sif": lambda: S.small_test_system("sif", nk=(2, 1, 2)),
 }
 
 

@@ -36,12 +36,12 @@ def test_library_rejects_bad_arguments_without_gpu():
     L = api.lib()
     assert L.olc_create(None, None, None) != 0
     assert L.olc_primitive_batch(9, 1, None, None, None) != 0
-    # f-type exponents are outside this build and report it
+    # g-type (l = 4) exponents are outside the kernels and report it
     out = np.zeros(256)
     p = np.zeros(12)
-    lm = np.array([16, 1], np.int32)
+    lm = np.array([25, 1], np.int32)
     st = L.olc_primitive_batch(1, 1, p.ctypes.data, lm.ctypes.data, out.ctypes.data)
-    assert st == 7 and "lmalpha" in api.last_error()
+    assert st == 1 and "lmalpha" in api.last_error()
 
 
 @pytest.mark.parametrize("name,nv,nc,nk", [
@@ -80,10 +80,10 @@ def test_reference_assembly_rule():
     assert np.allclose(h, 1 + 1 + 1 + 2)      # zero multiplier adds unscaled
 
 
-def test_f_functions_are_refused_by_the_gpu_build(gpu_free_lib):
-    """The device kernels are built for s, p, d; an f block is refused with
-    OLC_ERR_UNSUPPORTED before any device work (the oracle covers f)."""
+def test_g_functions_are_refused_by_the_gpu_build(gpu_free_lib):
+    """The device kernels are built for s, p, d, f; a radial function with
+    l = 4 is refused with OLC_ERR_ARG before any device work."""
     from olcao_gb300 import api
     with pytest.raises(api.OlcError) as e:
-        api.primitive_batch(1, np.zeros((1, 12)) + 1.0, np.array([[16, 1]], np.int32))
-    assert e.value.status == 7
+        api.primitive_batch(1, np.zeros((1, 12)) + 1.0, np.array([[25, 1]], np.int32))
+    assert e.value.status == 1
