@@ -460,8 +460,10 @@ def run_ours(args, world, rank, dist):
     asm_bytes = nk * ((2 + pd) * plen * 16 + n * n * 16)
     kernels = {
         # stage: (kernel, bound)
-        "tridiag": ("hetrd_kernel (FP32 Householder tridiagonalisation, one cluster per k)", "hbm"),
-        "split": ("tc_gemm_kernel<fixed> (tcgen05 split-digit products, FP64-accurate) + digit slicing", "tensor"),
+        "tridiag": ("hetrd_panel_kernel + tc_gemm_kernel<f32> trailing updates (blocked FP32 "
+                    "tridiagonalisation, one cluster per k)", "hbm"),
+        "split": ("tc_gemm_kernel<fixed> (tcgen05 8-bit split-digit products, FP64-accurate) + digit slicing",
+                  "tensor"),
         "backtransform": ("tc_gemm_kernel<f32> (tcgen05 compact-WY back-transform, X = U^-1 Z)", "tensor"),
         "assemble": ("assemble_full_kernel (H(k) from the resident packed operators)", "hbm"),
     }

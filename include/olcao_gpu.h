@@ -266,7 +266,8 @@ int olc_profile_read(olc_context_t* ctx, int stage, int64_t* launches, double* m
 /* Algorithmic work of a stage since the last reset: tensor-core flops issued
  * (the split and FP32-accurate products count every BF16 multiply-add) and
  * the streamed bytes of the HBM-bound kernels (tridiagonalisation: the
- * trailing triangle read and written at every step). */
+ * trailing triangle read once per step, and the lower triangles the
+ * between-panel updates read and write). */
 int olc_profile_read_work(olc_context_t* ctx, int stage, double* flops, double* bytes);
 /* Kernels of this library launched so far in the process (all contexts). */
 int64_t olc_launch_count(void);

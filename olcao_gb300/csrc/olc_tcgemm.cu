@@ -18,9 +18,10 @@
 // segments (plane of A, plane of B, K-block range):
 //
 //  * fixed mode (FP64-accurate products): every row of op(A) and column of B
-//    is scaled by a power of two and cut into signed 7-bit digits
-//    (|d| <= 127, exact in BF16).  One segment is one digit pair (s, t) over
-//    at most 1024 of K', so that its FP32 sum of at most 1024 * 127^2 < 2^24
+//    is scaled by a power of two and cut into signed 8-bit digits
+//    (|d| <= 255: BF16 holds every integer up to 256 exactly).  One segment is
+//    one digit pair (s, t) over at most 256 of K', so that its FP32 sum of at
+//    most 256 * 255^2 < 2^24
 //    is an exact integer.  Segments alternate between two TMEM accumulators;
 //    the epilogue drains each one (tcgen05.ld, exact float -> int) into
 //    64-bit fixed point, acc += g << shift(s + t), while the tensor cores fill
@@ -63,6 +64,10 @@ constexpr int MMA_WARP = NUM_EPI_WARPS + 1;
 template <int MODE>
 constexpr int tmem_cols() { return MODE == 0 ? 256 : 512; }
 constexpr long long kWaitNs = 2000000000LL;   // 2 s per wait
+// fixed mode: K' per drained segment, the largest multiple of BK with
+// kChunkK (2^kBeta - 1)^2 < 2^24 (every FP32 partial sum an exact integer)
+constexpr int kChunkK = (int)((16777215LL / (((1LL << kBeta) - 1) * ((1LL << kBeta) - 1))) / BK * BK);
+static_assert(kChunkK >= BK, "digit width too large for exact FP32 segments");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -222,6 +227,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   // Hermitian result: a tile whose complex columns all lie left of its first
   // row is wholly below the diagonal (filled afterwards from the upper part)
   if (p.herm_upper && (n0 >> 1) + BN / 2 - 1 < m0) return;
+  // lower part wanted: a tile whose complex columns all lie right of its last
+  // row is wholly above the diagonal
+  if (p.lower_only && (n0 >> 1) > m0 + BM - 1) return;
   // segments: every pair over K chunks of chunk_blocks K-blocks
   const int nchunk = (p.kblocks + p.chunk_blocks - 1) / p.chunk_blocks;
   const int nseg = p.npairs * nchunk;
@@ -698,10 +706,11 @@ int launch(olc_context* ctx, int mode, const void* dA, const void* dB, int plane
   }
   count_launch();
   double frac = 1.0;
-  if (p.herm_upper) {
+  if (p.herm_upper || p.lower_only) {
     long long done = 0;
     for (int mt = 0; mt < p.nmt; ++mt)
-      for (int nt = 0; nt < p.nnt; ++nt) done += ((nt * BN) / 2 + BN / 2 - 1 >= mt * BM);
+      for (int nt = 0; nt < p.nnt; ++nt)
+        done += p.herm_upper ? ((nt * BN) / 2 + BN / 2 - 1 >= mt * BM) : ((nt * BN) / 2 <= mt * BM + BM - 1);
     frac = (double)done / ((double)p.nmt * p.nnt);
   }
   add_work(ctx, stage, 2.0 * m * (double)nreal * (double)Kp * p.npairs * nb * frac, 0.0);
@@ -741,7 +750,7 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
   fixed_plan(bits_a, bits_b, std::max(bits_a, bits_b), &na, &nbd, &T);
   const int kp = (k + 31) & ~31;
   const size_t Kp = 2 * (size_t)kp;
-  // FP32-exact segments: at most 1024 of K' per drain
+  // FP32-exact segments: at most kChunkK of K' per drain
   std::vector<TcPair> pairs;
   for (int d = 0; d <= T; ++d)
     for (int s = 0; s < na; ++s) {
@@ -791,7 +800,7 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
     p.base = L - kBeta * (T + 2);
     p.npairs = (int)pairs.size();
     for (size_t i = 0; i < pairs.size(); ++i) p.pairs[i] = pairs[i];
-    p.chunk_blocks = 1024 / BK;
+    p.chunk_blocks = kChunkK / BK;
     p.herm_upper = hermitian ? 1 : 0;
     if ((s = launch(ctx, 0, wa, wb, na, nbd, Kp, m, 2 * n, cb, p, stage))) return s;
     if (hermitian) {
@@ -809,7 +818,7 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
 
 int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long sA, int lda, bool conjA,
               const float* B, long long sB, int ldb, float alpha, float beta, float* C, long long sC, int ldc,
-              int nb, int stage) {
+              int nb, int stage, bool lower) {
   cudaStream_t st = ctx->stream;
   const int kp = (k + 31) & ~31;
   const size_t Kp = 2 * (size_t)kp;
@@ -847,6 +856,7 @@ int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long s
     p.npairs = npairs;
     for (int i = 0; i < npairs; ++i) p.pairs[i] = TcPair{pairs[i][0], pairs[i][1], 0};
     p.chunk_blocks = 512 / BK;
+    p.lower_only = lower ? 1 : 0;
     if ((s = launch(ctx, 1, wa, wb, 3, 3, Kp, m, 2 * n, cb, p, stage))) return s;
   }
   cudaFreeAsync(wa, st);

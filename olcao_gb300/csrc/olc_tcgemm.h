@@ -8,7 +8,7 @@
 namespace olc {
 namespace tc {
 
-constexpr int kBeta = 7;         // bits per digit of the fixed-point split (|d| <= 127, exact in BF16)
+constexpr int kBeta = 8;         // bits per digit of the fixed-point split (|d| <= 255, exact in BF16)
 constexpr int kMaxPairs = 96;    // digit pairs (or BF16-piece pairs) per launch
 
 // One operand-plane pair of a launch; shift: int64 shift of its drained sums
@@ -33,12 +33,13 @@ struct TcParams {
   int nmt, nnt;                 // tiles
   int npairs, kblocks, chunk_blocks;   // segments: pairs x ceil(kblocks / chunk_blocks) K chunks
   int herm_upper;               // Hermitian result: tiles wholly below the diagonal are skipped
+  int lower_only;               // f32 mode: tiles wholly above the diagonal are skipped
   int* err;                     // device error word (expired waits)
   TcPair pairs[kMaxPairs];
 };
 
 // FP64-accurate complex product C[b] = op(A[b]) B[b] (m x n, column-major,
-// ld m) from 7-bit digit planes: bits_a / bits_b bits kept of A / B.
+// ld m) from 8-bit digit planes: bits_a / bits_b bits kept of A / B.
 // hermitian: the result is known to be Hermitian (m == n); only the tiles
 // that touch the upper triangle are computed and the strict lower triangle
 // is filled from it.
@@ -48,10 +49,12 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
                 bool hermitian = false);
 
 // FP32-accurate complex product C[b] = alpha op(A[b]) B[b] + beta C[b] from
-// three BF16 pieces per FP32 operand (six piece pairs).
+// three BF16 pieces per FP32 operand (six piece pairs).  lower: only the
+// output tiles that reach the lower triangle (row >= column) are formed; the
+// rest of C keeps its values.
 int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long sA, int lda, bool conjA,
               const float* B, long long sB, int ldb, float alpha, float beta, float* C, long long sC, int ldc,
-              int nb, int stage);
+              int nb, int stage, bool lower = false);
 
 // Digits and kept pairs of a fixed-point product (see olc_tcgemm.cu).
 void fixed_plan(int bits_a, int bits_b, int prec, int* na, int* nbd, int* T);

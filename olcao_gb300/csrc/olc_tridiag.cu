@@ -7,13 +7,14 @@
 //      FP32, computed once per prepared S); the two products run on the
 //      tensor cores (three BF16 pieces per FP32 operand, olc_tcgemm.cu).
 //   2. C = Q T Q^H by Householder reflectors H_i = I - tau_i v_i v_i^H, the
-//      lower-triangle reduction of LAPACK chetd2: one thread-block cluster per
-//      k owns the k's matrix in HBM, its CTAs own interleaved columns.  Every
-//      step i makes ONE pass over the trailing matrix that applies the pending
-//      rank-2 update of step i-1 (A -= v w^H + w v^H) and, in the same read,
-//      forms p = tau A v_i for step i.  The reflector vectors are broadcast and
-//      the products p exchanged through distributed shared memory; the cluster
-//      barrier orders the steps.
+//      lower-triangle reduction of LAPACK chetrd in its blocked form: panels
+//      of 32 reflectors, one thread-block cluster per k whose CTAs own
+//      interleaved columns and rows.  Inside a panel every step reads the
+//      trailing matrix once (no write-back: the panel's updates are held back
+//      as V, W and applied to the vectors, LAPACK clatrd); the reflector
+//      columns and the partial products cross CTAs through distributed shared
+//      memory, the cluster barrier orders the steps.  Between panels the
+//      trailing matrix takes the panel's rank-64 update on the tensor cores.
 //   3. T z = lambda z in FP64: eigenvalues by bisection on FP32 Sturm counts,
 //      eigenvectors by FP64 inverse iteration (LU with partial pivoting of
 //      T - sigma I, as LAPACK dstein), then modified Gram-Schmidt inside every
@@ -40,7 +41,6 @@ namespace olc {
 
 namespace {
 
-constexpr int kTrdThreads = 512;
 constexpr int kWyBlock = 128;        // reflectors per compact-WY block
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -85,98 +85,111 @@ __device__ __forceinline__ void block_sum2_d(double& a, double& b, double* red) 
 }
 
 // ---------------------------------------------------------------------------
-// 2. Householder tridiagonalisation, one cluster of G CTAs per k
+// 2. Householder tridiagonalisation in panels, one cluster of G CTAs per k
 // ---------------------------------------------------------------------------
-// A: [nk][n][n] complex FP32, column-major; only the lower triangle is read
-// or written.  On return column i holds v_i in rows i+1..n-1 (v_i(i+1) = 1),
-// d[k][i] the diagonal of T, e[k][i] its (real) off-diagonal, tau[k][i] the
-// reflector factors.  Column r belongs to CTA r % G of the cluster for the
-// whole reduction, so only the cluster's shared memory crosses CTAs.
+// The lower-triangle reduction of LAPACK chetrd in its blocked form.  A panel
+// of kTrdNb reflectors is formed by one hetrd_panel_kernel launch against the
+// matrix A_s as it stood at the panel's start, the panel's rank-2 updates held
+// back as V, W (A_cur = A_s - V W^H - W V^H, LAPACK clatrd); between panels
+// the trailing matrix receives them at once, A22 -= [V W] [W V]^H, an
+// FP32-accurate tensor-core product (olc_tcgemm.cu, lower tiles only).
+// While a panel runs, A is only read (and column i receives v_i), so the
+// HBM stream of each step is one read of the trailing lower triangle.
 //
-// Step i: (a) every CTA reads column i from L2, applies the pending update
-// of step i-1 and forms the reflector (v_i, tau_i) itself (no broadcast);
-// (b) each CTA streams its columns r > i once: element a = A(c, r), c >= r,
-// receives the pending update a -= v_{i-1}(c) conj(w_{i-1}(r)) +
-// w_{i-1}(c) conj(v_{i-1}(r)), is written back, and adds conj(a) v_i(c) to
-// (A v_i)(r) and, for c > r, a v_i(r) to (A v_i)(c) (shared-memory atomics);
-// (c) the partial products are summed over the cluster, p = tau_i A v_i,
-// together with the shares of p^H v_i, and w_i = p - tau_i/2 (p^H v_i) v_i
-// becomes the pending update; the owner of column i stores v_i there.  Two
-// cluster barriers per step.
+// A: [nk][n][ld] complex FP32, column-major; only the lower triangle is read
+// (the upper one holds stale values).  On return column i holds v_i in rows
+// i+1..n-1 (v_i(i+1) = 1), d[k][i] the diagonal of T, e[k][i] its (real)
+// off-diagonal, tau[k][i] the reflector factors.
+// XH, YH: [nk][n][2 kTrdNb]: row r of XH is [conj V(r, :) | conj W(r, :)],
+// of YH [conj W(r, :) | conj V(r, :)] -- the operands of the trailing update
+// in the K-major layout the tensor-core product reads as op(A) = A^H.
+//
+// Inside a cluster, column r and row r belong to CTA r % G.  Step i
+// (t = i - p0 within the panel):
+//  (a) each CTA forms the rows r >= i it owns of column i of A_cur (A_s(r, i)
+//      minus the held-back updates: a warp per row, a lane per reflector of
+//      the panel) and writes them into every CTA's copy of the column
+//      (distributed shared memory), with its share of ||x||^2;  cluster barrier
+//  (b) every CTA forms the reflector (v_i, tau_i) from the whole column and
+//      stores the rows it owns of v_i into column i of A; streams its columns
+//      r > i of A_s once, read only: conj(a) v_i(c) adds to (A_s v_i)(r) and,
+//      for c > r, a v_i(r) to (A_s v_i)(c) (shared-memory atomics); forms its
+//      rows' share of V^H v_i and W^H v_i (a warp per four columns of XH);
+//                                                                cluster barrier
+//  (c) sums the cluster's partial products for its rows:
+//      p = tau_i (A_s v_i - V (W^H v_i) - W (V^H v_i)), with its share of
+//      p^H v_i;                                                   cluster barrier
+//  (d) w_i = p - tau_i/2 (p^H v_i) v_i for its rows, into XH and YH.
+// Every CTA keeps the panel rows p0..p1-1 of V and W in shared memory: row i
+// of both gives the coefficients of column i in (a), so it forms p for the
+// panel rows itself.  The column buffer alternates between steps, so that the
+// writes of step i+1 into another CTA's buffer never meet that CTA's reads of
+// step i.
 //
 // Deterministic variant (DET): the partial products are accumulated in
 // 64-bit fixed point with integer shared-memory atomics, whose sum does not
 // depend on the order in which the warps add; the unit of step i is
 // 2^-60 of a bound on every partial sum, ||A||_F ||v_i|| (the Frobenius norm
-// of the whole matrix bounds the trailing one: the reflectors are unitary).
-// A rerun gives bit-identical reflectors.  It needs 40 bytes of shared
-// memory per row (the float variant 32), so the largest n run the float
-// variant.
-constexpr int kTrdPanel = 8;      // owned columns per warp and pass
+// of the whole matrix bounds every trailing matrix: the reflectors are
+// unitary).  Every other sum runs in a fixed order, so a rerun gives
+// bit-identical reflectors.  It needs 32 bytes of shared memory per row (the
+// float variant 24), so the largest n run the float variant.
+constexpr int kTrdThreads = 512;
+constexpr int kTrdWarps = kTrdThreads / 32;
+constexpr int kTrdNb = 32;        // reflectors per panel: one lane per reflector
+constexpr int kTrdXW = 2 * kTrdNb;  // row length of XH, YH
+constexpr int kTrdPanel = 8;      // owned columns per warp and pass of the product
+constexpr int kTrdMaxG = 16;
+static_assert(4 * kTrdWarps == kTrdXW, "a warp per four columns of XH");
 
-// Destination of the partial products A v_i of one CTA.
+// Destination of the partial products A v_i of one CTA.  The sums of row c
+// live in four planes of ld/2 words -- (re, even rows), (re, odd rows),
+// (im, even rows), (im, odd rows) -- at word c/2, so that the lanes of a warp,
+// which add to consecutive row pairs, touch consecutive words.
 struct TrdAcc {
-  float2* w;                      // float variant: shared-memory float sums
-  unsigned long long* q;          // DET: fixed-point sums [2 * row] (re, im)
+  float* f;                       // float variant: shared-memory float sums
+  unsigned long long* q;          // DET: fixed-point sums
   float scale;                    // DET: 1 / unit (a power of two)
+  int h;                          // words per plane (ld / 2)
 };
+
+__device__ __forceinline__ int acc_re(int c, int h) { return (c & 1) * h + (c >> 1); }
+__device__ __forceinline__ int acc_im(int c, int h) { return (2 + (c & 1)) * h + (c >> 1); }
 
 template <bool DET>
 __device__ __forceinline__ void acc_add(const TrdAcc& a, int c, float x, float y) {
   if (DET) {
-    atomicAdd(&a.q[2 * c], (unsigned long long)__float2ll_rn(x * a.scale));
-    atomicAdd(&a.q[2 * c + 1], (unsigned long long)__float2ll_rn(y * a.scale));
+    atomicAdd(&a.q[acc_re(c, a.h)], (unsigned long long)__float2ll_rn(x * a.scale));
+    atomicAdd(&a.q[acc_im(c, a.h)], (unsigned long long)__float2ll_rn(y * a.scale));
   } else {
-    atomicAdd(&a.w[c].x, x);
-    atomicAdd(&a.w[c].y, y);
+    atomicAdd(&a.f[acc_re(c, a.h)], x);
+    atomicAdd(&a.f[acc_im(c, a.h)], y);
   }
 }
 
-// One row pair (2q, 2q+1) of a panel: pending update, write-back, column
-// products and the pair's mirrored products.  MASK: the pair may lie on or
-// above a panel column's diagonal.
-template <bool DET, bool PEND, bool MASK>
-__device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int ld, int q,
-                                         const int (&cr)[kTrdPanel], const float2* __restrict__ vP,
-                                         const float2* __restrict__ wP, const float2 (&vr)[kTrdPanel],
-                                         float (&ax)[kTrdPanel], float (&ay)[kTrdPanel],
-                                         const float4* __restrict__ vP4, const float4* __restrict__ wP4,
-                                         const float4* __restrict__ vC4, const TrdAcc& wC) {
+// One row pair (2q, 2q+1) of a set of owned columns, the matrix values
+// already loaded: the columns' products and the pair's mirrored products.
+// MASK: the pair may lie on or above a column's diagonal.
+template <bool DET, bool MASK>
+__device__ __forceinline__ void trd_pair(const float4 (&a4)[kTrdPanel], int n, int q, const int (&cr)[kTrdPanel],
+                                         const float2 (&vr)[kTrdPanel], float (&ax)[kTrdPanel],
+                                         float (&ay)[kTrdPanel], const float4 vc, const TrdAcc& acc) {
   const int c0 = 2 * q;
-  float4 a4[kTrdPanel];
-#pragma unroll
-  for (int t = 0; t < kTrdPanel; ++t)
-    a4[t] = (cr[t] < n && (!MASK || cr[t] <= c0 + 1))
-                ? reinterpret_cast<const float4*>(Ak + (size_t)cr[t] * ld)[q]
-                : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 vc = vC4[q];
-  float4 vp = make_float4(0.f, 0.f, 0.f, 0.f), wp = vp;
-  if (PEND) { vp = vP4[q]; wp = wP4[q]; }
   float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f;
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
     if (cr[t] >= n || (MASK && cr[t] > c0 + 1)) continue;
     float2 a0 = make_float2(a4[t].x, a4[t].y), a1 = make_float2(a4[t].z, a4[t].w);
-    if (PEND) {
-      // conj(w(r)) and conj(v(r)) of this column (shared-memory broadcast)
-      const float2 cw = conjf2(wP[cr[t]]), cv = conjf2(vP[cr[t]]);
-      a0.x -= (vp.x * cw.x - vp.y * cw.y) + (wp.x * cv.x - wp.y * cv.y);
-      a0.y -= (vp.x * cw.y + vp.y * cw.x) + (wp.x * cv.y + wp.y * cv.x);
-      a1.x -= (vp.z * cw.x - vp.w * cw.y) + (wp.z * cv.x - wp.w * cv.y);
-      a1.y -= (vp.z * cw.y + vp.w * cw.x) + (wp.z * cv.y + wp.w * cv.x);
+    if (MASK) {                     // the diagonal is real
+      if (c0 == cr[t]) a0.y = 0.f;
+      if (c0 + 1 == cr[t]) a1.y = 0.f;
     }
-    const bool m0 = !MASK || c0 >= cr[t];
-    if (m0) {
+    if (!MASK || c0 >= cr[t]) {
       ax[t] += a0.x * vc.x + a0.y * vc.y;         // conj(a) v
       ay[t] += a0.x * vc.y - a0.y * vc.x;
     }
     ax[t] += a1.x * vc.z + a1.y * vc.w;
     ay[t] += a1.x * vc.w - a1.y * vc.z;
-    float2* colt = Ak + (size_t)cr[t] * ld;
-    if (PEND) {
-      if (m0) reinterpret_cast<float4*>(colt)[q] = make_float4(a0.x, a0.y, a1.x, a1.y);
-      else colt[c0 + 1] = a1;
-    }
     if (!MASK || c0 > cr[t]) {
       s0x += a0.x * vr[t].x - a0.y * vr[t].y;
       s0y += a0.x * vr[t].y + a0.y * vr[t].x;
@@ -186,19 +199,21 @@ __device__ __forceinline__ void trd_pair(float2* __restrict__ Ak, int n, int ld,
       s1y += a1.x * vr[t].y + a1.y * vr[t].x;
     }
   }
-  if (!MASK || s0x != 0.f || s0y != 0.f) acc_add<DET>(wC, c0, s0x, s0y);
-  if (!MASK || s1x != 0.f || s1y != 0.f) acc_add<DET>(wC, c0 + 1, s1x, s1y);
+  if (!MASK || s0x != 0.f || s0y != 0.f) acc_add<DET>(acc, c0, s0x, s0y);
+  if (!MASK || s1x != 0.f || s1y != 0.f) acc_add<DET>(acc, c0 + 1, s1x, s1y);
 }
 
-// One panel of kTrdPanel owned columns (slots past the last column are
-// empty): the pairs touching the diagonals first, then the bulk unmasked.
-template <bool DET, bool PEND>
-__device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld, int r0, int G, int pn, int nown,
-                                          int lane, const float2* vP, const float2* wP, const float2* vC,
-                                          const TrdAcc& wC) {
+// One set of kTrdPanel owned columns (slots past the last column are empty):
+// the pairs touching the diagonals first, then the bulk unmasked with two
+// pairs per lane in flight.  A_s is read through the non-coherent path: the
+// kernel writes only column i, which no product reads.
+template <bool DET>
+__device__ __forceinline__ void trd_columns(const float2* __restrict__ Ak, int n, int ld, int r0, int G, int pn,
+                                            int nown, int lane, const float2* vC, const TrdAcc& acc) {
   int cr[kTrdPanel];
   float2 vr[kTrdPanel];
   float ax[kTrdPanel], ay[kTrdPanel];
+  int off[kTrdPanel];                           // column offsets in float4 units
   int c_last = 0;
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
@@ -209,15 +224,37 @@ __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld
     vr[t] = vC[rr];
     ax[t] = 0.f;
     ay[t] = 0.f;
+    off[t] = rr * (ld >> 1);
   }
-  const float4* vP4 = reinterpret_cast<const float4*>(vP);
-  const float4* wP4 = reinterpret_cast<const float4*>(wP);
+  const float4* A4 = reinterpret_cast<const float4*>(Ak);
   const float4* vC4 = reinterpret_cast<const float4*>(vC);
   const int q1 = ld >> 1;                       // the last pair may hold the zero padding row
   const int qd = min(q1, (c_last >> 1) + 1);    // pairs from qd on lie below every diagonal
   int q = (cr[0] >> 1) + lane;
-  for (; q < qd; q += 32) trd_pair<DET, PEND, true>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
-  for (; q < q1; q += 32) trd_pair<DET, PEND, false>(Ak, n, ld, q, cr, vP, wP, vr, ax, ay, vP4, wP4, vC4, wC);
+  for (; q < qd; q += 32) {
+    float4 a4[kTrdPanel];
+#pragma unroll
+    for (int t = 0; t < kTrdPanel; ++t)
+      a4[t] = (cr[t] < n && cr[t] <= 2 * q + 1) ? __ldg(A4 + off[t] + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    trd_pair<DET, true>(a4, n, q, cr, vr, ax, ay, vC4[q], acc);
+  }
+  // the pairs below every diagonal: two pairs per lane in flight
+  for (; q + 32 < q1; q += 64) {
+    float4 a4[kTrdPanel], b4[kTrdPanel];
+#pragma unroll
+    for (int t = 0; t < kTrdPanel; ++t) {
+      a4[t] = cr[t] < n ? __ldg(A4 + off[t] + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+      b4[t] = cr[t] < n ? __ldg(A4 + off[t] + q + 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    trd_pair<DET, false>(a4, n, q, cr, vr, ax, ay, vC4[q], acc);
+    trd_pair<DET, false>(b4, n, q + 32, cr, vr, ax, ay, vC4[q + 32], acc);
+  }
+  if (q < q1) {
+    float4 a4[kTrdPanel];
+#pragma unroll
+    for (int t = 0; t < kTrdPanel; ++t) a4[t] = cr[t] < n ? __ldg(A4 + off[t] + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    trd_pair<DET, false>(a4, n, q, cr, vr, ax, ay, vC4[q], acc);
+  }
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
     float x = ax[t], y = ay[t];
@@ -225,222 +262,372 @@ __device__ __forceinline__ void trd_panel(float2* __restrict__ Ak, int n, int ld
       x += __shfl_xor_sync(0xffffffffu, x, o);
       y += __shfl_xor_sync(0xffffffffu, y, o);
     }
-    if (lane == 0 && cr[t] < n) acc_add<DET>(wC, cr[t], x, y);
+    if (lane == 0 && cr[t] < n) acc_add<DET>(acc, cr[t], x, y);
   }
 }
 
+// Cluster sum of the partial products of row c (in rank order; the remote
+// loads of all CTAs are issued together).
 template <bool DET>
-__global__ void __launch_bounds__(kTrdThreads) hetrd_kernel(float2* __restrict__ A, int n, int ld,
-                                                            double* __restrict__ dout,
-                                                            double* __restrict__ eout,
-                                                            float2* __restrict__ tout) {
+__device__ __forceinline__ float2 trd_row_sum(cg::cluster_group& cl, int G, int c, const TrdAcc& a, double unit) {
+  const int jr = acc_re(c, a.h), ji = acc_im(c, a.h);
+  if constexpr (DET) {
+    long long qr = 0, qi = 0;     // integer sums: the same in any order
+#pragma unroll
+    for (int g = 0; g < kTrdMaxG; ++g)
+      if (g < G) {
+        const unsigned long long* qg = cl.map_shared_rank(a.q, g);
+        qr += (long long)qg[jr];
+        qi += (long long)qg[ji];
+      }
+    return make_float2((float)((double)qr * unit), (float)((double)qi * unit));
+  } else {
+  float ur[kTrdMaxG], ui[kTrdMaxG];
+#pragma unroll
+  for (int g = 0; g < kTrdMaxG; ++g) {
+    ur[g] = 0.f;
+    ui[g] = 0.f;
+    if (g < G) {
+      const float* fg = cl.map_shared_rank(a.f, g);
+      ur[g] = fg[jr];
+      ui[g] = fg[ji];
+    }
+  }
+  float2 u = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int g = 0; g < kTrdMaxG; ++g) {
+    u.x += ur[g];
+    u.y += ui[g];
+  }
+  return u;
+  }
+}
+
+// The product p of an owned row past the panel, kept in the row's own sum
+// words (only the owner reads the sums of such a row).
+template <bool DET>
+__device__ __forceinline__ void trd_keep(const TrdAcc& a, int c, float2 p) {
+  if (DET) {
+    a.q[acc_re(c, a.h)] = __float_as_uint(p.x);
+    a.q[acc_im(c, a.h)] = __float_as_uint(p.y);
+  } else {
+    a.f[acc_re(c, a.h)] = p.x;
+    a.f[acc_im(c, a.h)] = p.y;
+  }
+}
+template <bool DET>
+__device__ __forceinline__ float2 trd_kept(const TrdAcc& a, int c) {
+  if (DET) return make_float2(__uint_as_float((unsigned)a.q[acc_re(c, a.h)]), __uint_as_float((unsigned)a.q[acc_im(c, a.h)]));
+  return make_float2(a.f[acc_re(c, a.h)], a.f[acc_im(c, a.h)]);
+}
+
+__device__ __forceinline__ float2 warp_sum2(float2 s) {
+  for (int o = 16; o; o >>= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+  }
+  return s;
+}
+
+// First row >= x owned by CTA `rank` of G.
+__device__ __forceinline__ int trd_first_owned(int x, int rank, int G) { return x + ((rank - x) % G + G) % G; }
+
+struct TrdArgs {
+  float2* A;
+  float2* XH;
+  float2* YH;
+  double* d;
+  double* e;
+  float2* tau;
+  double* fro;          // [nk] ||A||_F of the matrix entering the first panel
+  int n, ld, p0, nbp;   // panel: steps p0 .. p0 + nbp - 1
+};
+
+template <bool DET>
+__global__ void __launch_bounds__(kTrdThreads, 1) hetrd_panel_kernel(const __grid_constant__ TrdArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   const int G = (int)cl.num_blocks();
   const int rank = (int)cl.block_rank();
   const int k = blockIdx.y;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  float2* Ak = A + (size_t)k * n * ld;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n = a.n, ld = a.ld, p0 = a.p0, p1 = a.p0 + a.nbp;
+  float2* Ak = a.A + (size_t)k * n * ld;
+  float2* XHk = a.XH + (size_t)k * n * kTrdXW;
+  float2* YHk = a.YH + (size_t)k * n * kTrdXW;
   extern __shared__ float4 trd_sm4[];
-  float2* trd_sm = reinterpret_cast<float2*>(trd_sm4);
-  // float variant: [v_a | w_a | v_b | w_b], (v, w) pairs alternating between steps;
-  // DET: [v_a | v_b | w | fixed-point sums (2 ld int64)]
-  unsigned long long* qsum = reinterpret_cast<unsigned long long*>(trd_sm + 3 * (size_t)ld);
+  float2* vbuf = reinterpret_cast<float2*>(trd_sm4);                 // [2][ld] column / reflector
+  float* fsum = reinterpret_cast<float*>(vbuf + 2 * (size_t)ld);       // float variant: [4][ld / 2]
+  unsigned long long* qsum = reinterpret_cast<unsigned long long*>(fsum);   // DET: [4][ld / 2]
+  __shared__ float2 Vp[kTrdNb][kTrdNb], Wp[kTrdNb][kTrdNb];   // panel rows of V, W: [row - p0][t]
+  __shared__ float2 ypart[kTrdXW], ysum[kTrdXW], pp[kTrdNb];
+  __shared__ double s_nrm[kTrdMaxG], s_frp[kTrdMaxG];
+  __shared__ double2 s_dot[kTrdMaxG];
   __shared__ double red[72];
-  __shared__ float2 s_tau, s_scale;
+  __shared__ float2 s_tau, s_scale, s_al2;
   __shared__ float s_diag, s_beta, s_qscale;
   __shared__ double s_unit, s_fro;
-  __shared__ double2 s_dot[16];
-  for (int e = tid; e < (DET ? 5 : 4) * ld; e += blockDim.x) trd_sm[e] = make_float2(0.f, 0.f);
-  if (DET) {
+  for (int x = tid; x < (DET ? 4 : 3) * ld; x += blockDim.x) vbuf[x] = make_float2(0.f, 0.f);
+  for (int x = tid; x < kTrdNb * kTrdNb; x += blockDim.x) {
+    (&Vp[0][0])[x] = make_float2(0.f, 0.f);
+    (&Wp[0][0])[x] = make_float2(0.f, 0.f);
+  }
+  if (DET && p0 == 0) {
     // ||A||_F of the lower-triangle storage (off-diagonal entries twice)
     double part = 0.0;
     for (int c = rank; c < n; c += G) {
-      const float2* col = Ak + (size_t)c * ld;
+      const float2* colc = Ak + (size_t)c * ld;
       for (int r = c + tid; r < n; r += blockDim.x) {
-        const float2 a = col[r];
-        part += (r == c ? 1.0 : 2.0) * ((double)a.x * a.x + (double)a.y * a.y);
+        const float2 v = colc[r];
+        part += (r == c ? 1.0 : 2.0) * ((double)v.x * v.x + (double)v.y * v.y);
       }
     }
     const double f2 = block_sum_d(part, red);
-    if (tid == 0)
-      for (int g = 0; g < G; ++g) cl.map_shared_rank(s_dot, g)[rank] = make_double2(f2, 0.0);
+    if (tid < G) cl.map_shared_rank(s_frp, tid)[rank] = f2;
   }
   __syncthreads();
   cl.sync();
   if (DET && tid == 0) {
-    double f2 = 0.0;
-    for (int g = 0; g < G; ++g) f2 += s_dot[g].x;
-    s_fro = sqrt(f2);
+    if (p0 == 0) {
+      double f2 = 0.0;
+      for (int g = 0; g < G; ++g) f2 += s_frp[g];
+      s_fro = sqrt(f2);
+      if (rank == 0) a.fro[k] = s_fro;
+    } else {
+      s_fro = a.fro[k];
+    }
   }
   int cur = 0;
-  bool pend = false;
-  for (int i = 0; i < n - 1; ++i) {
-    float2 *vC, *wC, *wP;
-    const float2* vP;
-    if (DET) {
-      vC = trd_sm + (size_t)cur * ld;                  // v_i
-      vP = trd_sm + (size_t)(1 - cur) * ld;            // pending v_{i-1}
-      wP = trd_sm + 2 * (size_t)ld;                    // pending w_{i-1}, then w_i
-      wC = wP;
-    } else {
-      vC = trd_sm + (size_t)(2 * cur) * ld;            // v_i
-      wC = trd_sm + (size_t)(2 * cur + 1) * ld;        // partial A v_i, then w_i
-      vP = trd_sm + (size_t)(2 * (1 - cur)) * ld;      // pending v_{i-1}
-      wP = trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;  // pending w_{i-1}
-    }
-    // ---- (a) every CTA: pending update of column i, reflector of column i ----
-    // (column i is read from L2 by all CTAs; its owner writes v_i back only
-    // after the next cluster barrier)
+  for (int i = p0; i < p1; ++i) {
+    const int t = i - p0;
+    float2* vC = vbuf + (size_t)cur * ld;
+    // ---- (a) the owned rows of column i of A_cur, broadcast ---------------------
     {
-      const float2* col = Ak + (size_t)i * ld;
-      float2 cw = make_float2(0.f, 0.f), cv = cw;
-      if (pend) { cw = conjf2(wP[i]); cv = conjf2(vP[i]); }
+      // thread per owned row: x = A_s(r, i) - sum_u V(r, u) conj W(i, u) + W(r, u) conj V(i, u)
+      //                         = A_s(r, i) - conj(sum_u xv(u) W(i, u) + xw(u) V(i, u))
       double part = 0.0;
-      for (int r = i + tid; r < n; r += blockDim.x) {
-        float2 a = col[r];
-        if (pend) {
-          const float2 t1 = cmul(vP[r], cw), t2 = cmul(wP[r], cv);
-          a.x -= t1.x + t2.x;
-          a.y -= t1.y + t2.y;
+      for (int r = trd_first_owned(i, rank, G) + tid * G; r < n; r += blockDim.x * G) {
+        float2 x = Ak[(size_t)i * ld + r];
+        const float2* xr = XHk + (size_t)r * kTrdXW;
+        float sx = 0.f, sy = 0.f;
+#pragma unroll 4
+        for (int u = 0; u < t; ++u) {
+          const float2 xv = xr[u], xw = xr[kTrdNb + u], wq = Wp[t][u], vq = Vp[t][u];
+          sx += (xv.x * wq.x - xv.y * wq.y) + (xw.x * vq.x - xw.y * vq.y);
+          sy += (xv.x * wq.y + xv.y * wq.x) + (xw.x * vq.y + xw.y * vq.x);
         }
-        if (r == i) s_diag = a.x;
-        else vC[r] = a;
-        if (r >= i + 2) part += (double)a.x * a.x + (double)a.y * a.y;
+        x.x -= sx;
+        x.y += sy;
+#pragma unroll
+        for (int g = 0; g < kTrdMaxG; ++g)
+          if (g < G) cl.map_shared_rank(vC, g)[r] = x;
+        if (r >= i + 2) part += (double)x.x * x.x + (double)x.y * x.y;
       }
       const double xn2 = block_sum_d(part, red);
-      if (tid == 0) {
-        const float2 al = vC[i + 1];
-        float2 tau = make_float2(0.f, 0.f), scale = make_float2(0.f, 0.f);
-        float beta = al.x;
-        double vnorm2 = 1.0;
-        if (!(xn2 == 0.0 && al.y == 0.f)) {
-          const float an = sqrtf(al.x * al.x + al.y * al.y + (float)xn2);
-          beta = (al.x >= 0.f) ? -an : an;
-          tau = make_float2((beta - al.x) / beta, -al.y / beta);
-          const float dr = al.x - beta, di = al.y, den = dr * dr + di * di;
-          scale = make_float2(dr / den, -di / den);
-          vnorm2 = 1.0 + xn2 / (double)den;
-        }
-        s_tau = tau;
-        s_scale = scale;
-        s_beta = beta;
-        if (DET) {
-          // unit 2^(E - 60) with 2^E >= 2 ||A||_F ||v_i||
-          int E;
-          frexp(2.0 * s_fro * sqrt(vnorm2) + 1e-300, &E);
-          E = max(E, -60);
-          s_unit = ldexp(1.0, E - 60);
-          s_qscale = ldexpf(1.f, 60 - E);
-        }
+      if (tid < G) cl.map_shared_rank(s_nrm, tid)[rank] = xn2;
+    }
+    __syncthreads();
+    cl.sync();
+    // ---- (b) reflector; v_i into column i; products with A_s, V, W ------------------
+    if (tid == 0) {
+      double xn2 = 0.0;
+      for (int g = 0; g < G; ++g) xn2 += s_nrm[g];
+      s_diag = vC[i].x;
+      const float2 al = vC[i + 1];
+      float2 tau = make_float2(0.f, 0.f), scale = make_float2(0.f, 0.f);
+      float beta = al.x;
+      double vnorm2 = 1.0;
+      if (!(xn2 == 0.0 && al.y == 0.f)) {
+        const float an = sqrtf(al.x * al.x + al.y * al.y + (float)xn2);
+        beta = (al.x >= 0.f) ? -an : an;
+        tau = make_float2((beta - al.x) / beta, -al.y / beta);
+        const float dr = al.x - beta, di = al.y, den = dr * dr + di * di;
+        scale = make_float2(dr / den, -di / den);
+        vnorm2 = 1.0 + xn2 / (double)den;
       }
-      __syncthreads();
+      s_tau = tau;
+      s_scale = scale;
+      s_beta = beta;
+      if (DET) {
+        // unit 2^(E - 60) with 2^E >= 2 ||A||_F ||v_i||
+        int E;
+        frexp(2.0 * s_fro * sqrt(vnorm2) + 1e-300, &E);
+        E = max(E, -60);
+        s_unit = ldexp(1.0, E - 60);
+        s_qscale = ldexpf(1.f, 60 - E);
+      }
+    }
+    __syncthreads();
+    {
       const float2 scale = s_scale;
       for (int r = i + 1 + tid; r < n; r += blockDim.x)
         vC[r] = (r == i + 1) ? make_float2(1.f, 0.f) : cmul(vC[r], scale);
-      __syncthreads();
+      if (tid == 0) vC[i] = make_float2(0.f, 0.f);
     }
-    // ---- (b) one pass over the owned columns' lower parts -------------------
-    const float2 tau = s_tau;
-    int r0 = i + 1;
-    r0 += ((rank - r0) % G + G) % G;
+    __syncthreads();
+    const int r0 = trd_first_owned(i + 1, rank, G);
+    for (int r = r0 + tid * G; r < n; r += blockDim.x * G) Ak[(size_t)i * ld + r] = vC[r];
     {
-      // panels of kTrdPanel owned columns per warp; lane-owned row pairs
-      // (2q, 2q+1) collect the mirrored products of the whole panel in
-      // registers before one shared-memory atomic
-      const TrdAcc acc{wC, qsum, DET ? s_qscale : 1.f};
+      const TrdAcc acc{fsum, qsum, DET ? s_qscale : 1.f, ld >> 1};
       const int nown = r0 < n ? (n - r0 + G - 1) / G : 0;
       const int npanel = (nown + kTrdPanel - 1) / kTrdPanel;
-      for (int pn = warp; pn < npanel; pn += nwarps) {
-        if (pend) trd_panel<DET, true>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, acc);
-        else trd_panel<DET, false>(Ak, n, ld, r0, G, pn, nown, lane, vP, wP, vC, acc);
+      for (int pn = warp; pn < npanel; pn += kTrdWarps) trd_columns<DET>(Ak, n, ld, r0, G, pn, nown, lane, vC, acc);
+    }
+    {
+      // this CTA's share of XH^T v over its rows r > i: warp w takes columns 4w..4w+3
+      const int c4 = 4 * warp, u0 = c4 % kTrdNb;
+      float2 y[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) y[j] = make_float2(0.f, 0.f);
+      if (u0 < t) {
+#pragma unroll 4
+        for (int r = r0 + lane * G; r < n; r += 32 * G) {
+          const float4* xr = reinterpret_cast<const float4*>(XHk + (size_t)r * kTrdXW + c4);
+          const float4 q0 = xr[0], q1 = xr[1];
+          const float2 vr = vC[r];
+          const float2 z[4] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
+                               make_float2(q1.z, q1.w)};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float2 m = cmul(z[j], vr);
+            y[j].x += m.x;
+            y[j].y += m.y;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) y[j] = warp_sum2(y[j]);
       }
+      if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ypart[c4 + j] = (u0 + j < t) ? y[j] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     cl.sync();
-    // ---- (c) cluster sum of the partial products, p = tau A v, with the
-    // partial p^H v of this CTA's share; w_i = p + alpha v, alpha = -tau/2 p^H v
+    // ---- (c) p = tau (A_s v - V (W^H v) - W (V^H v)) ------------------------------
+    if (tid < kTrdXW) {
+      float2 u[kTrdMaxG];
+#pragma unroll
+      for (int g = 0; g < kTrdMaxG; ++g) u[g] = g < G ? cl.map_shared_rank(ypart, g)[tid] : make_float2(0.f, 0.f);
+      float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int g = 0; g < kTrdMaxG; ++g) {
+        s.x += u[g].x;
+        s.y += u[g].y;
+      }
+      ysum[tid] = s;
+    }
+    __syncthreads();
     {
-      int c0 = i + 1;
-      c0 += ((rank - c0) % G + G) % G;
-      double sx = 0.0, sy = 0.0;
+      const float2 tau = s_tau;
       const double unit = DET ? s_unit : 0.0;
-      for (int c = c0 + tid * G; c < n; c += blockDim.x * G) {
-        float2 t = make_float2(0.f, 0.f);
-        if (DET) {
-          long long qr = 0, qi = 0;      // integer sums: the same in any order
-          for (int g = 0; g < G; ++g) {
-            const unsigned long long* qg = cl.map_shared_rank(qsum, g);
-            qr += (long long)qg[2 * c];
-            qi += (long long)qg[2 * c + 1];
-          }
-          t = make_float2((float)((double)qr * unit), (float)((double)qi * unit));
-        } else {
-          for (int g = 0; g < G; ++g) {
-            const float2 u = cl.map_shared_rank(wC, g)[c];
-            t.x += u.x;
-            t.y += u.y;
-          }
+      const TrdAcc sums{fsum, qsum, 1.f, ld >> 1};
+      // ysum[nb + u] = (W^H v)(u), ysum[u] = (V^H v)(u)
+      double sx = 0.0, sy = 0.0;
+      // thread per row.  Panel rows (every CTA): V, W from the tables
+      for (int c = i + 1 + tid; c < p1; c += blockDim.x) {
+        const float2 P = trd_row_sum<DET>(cl, G, c, sums, unit);
+        float qx = 0.f, qy = 0.f;
+        for (int u = 0; u < t; ++u) {
+          const float2 t1 = cmul(Vp[c - p0][u], ysum[kTrdNb + u]), t2 = cmul(Wp[c - p0][u], ysum[u]);
+          qx += t1.x + t2.x;
+          qy += t1.y + t2.y;
         }
-        t = cmul(tau, t);
+        const float2 p = cmul(tau, make_float2(P.x - qx, P.y - qy));
+        pp[c - p0] = p;
+        if (c % G == rank) {
+          const float2 v = vC[c];
+          sx += (double)p.x * v.x + (double)p.y * v.y;
+          sy += (double)p.x * v.y - (double)p.y * v.x;
+        }
+      }
+      // owned rows past the panel: V, W from XH; p kept in the row's own sum
+      // slot (only the owner reads the sums of a row past the panel)
+      for (int c = trd_first_owned(max(i + 1, p1), rank, G) + tid * G; c < n; c += blockDim.x * G) {
+        const float2 P = trd_row_sum<DET>(cl, G, c, sums, unit);
+        const float2* xr = XHk + (size_t)c * kTrdXW;
+        float qx = 0.f, qy = 0.f;
+#pragma unroll 4
+        for (int u = 0; u < t; ++u) {
+          // V(c, u) (W^H v)(u) + W(c, u) (V^H v)(u), V = conj(xv), W = conj(xw)
+          const float2 t1 = cmul(conjf2(xr[u]), ysum[kTrdNb + u]), t2 = cmul(conjf2(xr[kTrdNb + u]), ysum[u]);
+          qx += t1.x + t2.x;
+          qy += t1.y + t2.y;
+        }
+        const float2 p = cmul(tau, make_float2(P.x - qx, P.y - qy));
+        trd_keep<DET>(sums, c, p);
         const float2 v = vC[c];
-        sx += (double)t.x * v.x + (double)t.y * v.y;
-        sy += (double)t.x * v.y - (double)t.y * v.x;
-        for (int g = 0; g < G; ++g) cl.map_shared_rank(wC, g)[c] = t;
+        sx += (double)p.x * v.x + (double)p.y * v.y;
+        sy += (double)p.x * v.y - (double)p.y * v.x;
       }
       block_sum2_d(sx, sy, red);
-      if (tid == 0)
-        for (int g = 0; g < G; ++g) cl.map_shared_rank(s_dot, g)[rank] = make_double2(sx, sy);
+      if (tid < G) cl.map_shared_rank(s_dot, tid)[rank] = make_double2(sx, sy);
     }
+    __syncthreads();
     cl.sync();
-    {
+    // ---- (d) w = p + alpha v with alpha = -tau/2 p^H v ------------------------------
+    if (tid == 0) {
+      const float2 tau = s_tau;
       double sx = 0.0, sy = 0.0;
-      for (int g = 0; g < G; ++g) { sx += s_dot[g].x; sy += s_dot[g].y; }
-      const float2 al2 = make_float2((float)(-0.5 * (tau.x * sx - tau.y * sy)),
-                                     (float)(-0.5 * (tau.x * sy + tau.y * sx)));
-      for (int c = i + 1 + tid; c < n; c += blockDim.x) {
-        const float2 t = cmul(al2, vC[c]);
-        wC[c].x += t.x;
-        wC[c].y += t.y;
+      for (int g = 0; g < G; ++g) {
+        sx += s_dot[g].x;
+        sy += s_dot[g].y;
       }
-      if (DET) {
-        // every CTA has read this CTA's sums (cluster barrier above)
-        for (int c = i + tid; c < n; c += blockDim.x) {
-          qsum[2 * c] = 0ULL;
-          qsum[2 * c + 1] = 0ULL;
-        }
-      } else {
-        for (int c = i + tid; c < n; c += blockDim.x) wP[c] = make_float2(0.f, 0.f);
-      }
-      // the owner stores the reflector and T's entries
-      if (rank == i % G) {
-        float2* col = Ak + (size_t)i * ld;
-        for (int r = i + 1 + tid; r < n; r += blockDim.x) col[r] = vC[r];
-        if (tid == 0) {
-          dout[(size_t)k * n + i] = s_diag;
-          eout[(size_t)k * (n - 1) + i] = s_beta;
-          tout[(size_t)k * (n - 1) + i] = tau;
-        }
+      s_al2 = make_float2((float)(-0.5 * (tau.x * sx - tau.y * sy)), (float)(-0.5 * (tau.x * sy + tau.y * sx)));
+      if (rank == 0) {
+        a.d[(size_t)k * n + i] = s_diag;
+        a.e[(size_t)k * (n - 1) + i] = s_beta;
+        a.tau[(size_t)k * (n - 1) + i] = tau;
       }
     }
     __syncthreads();
-    pend = true;
+    {
+      const float2 al2 = s_al2;
+      const TrdAcc sums{fsum, qsum, 1.f, ld >> 1};
+      for (int c = trd_first_owned(p0, rank, G) + tid * G; c < n; c += blockDim.x * G) {
+        float2 xv = make_float2(0.f, 0.f), xw = xv;     // conj v(c), conj w(c)
+        if (c > i) {
+          const float2 v = vC[c];
+          const float2 p = c < p1 ? pp[c - p0] : trd_kept<DET>(sums, c);
+          const float2 m = cmul(al2, v);
+          xv = conjf2(v);
+          xw = make_float2(p.x + m.x, -(p.y + m.y));
+        }
+        XHk[(size_t)c * kTrdXW + t] = xv;
+        XHk[(size_t)c * kTrdXW + kTrdNb + t] = xw;
+        YHk[(size_t)c * kTrdXW + t] = xw;
+        YHk[(size_t)c * kTrdXW + kTrdNb + t] = xv;
+      }
+      for (int c = i + 1 + tid; c < p1; c += blockDim.x) {
+        const float2 v = vC[c], m = cmul(al2, v), p = pp[c - p0];
+        Vp[c - p0][t] = v;
+        Wp[c - p0][t] = make_float2(p.x + m.x, p.y + m.y);
+      }
+    }
+    __syncthreads();
+    // every CTA has read this CTA's sums (cluster barrier above)
+    for (int c = i + tid; c < ld; c += blockDim.x) {
+      if (DET) {
+        qsum[acc_re(c, ld >> 1)] = 0ULL;
+        qsum[acc_im(c, ld >> 1)] = 0ULL;
+      } else {
+        fsum[acc_re(c, ld >> 1)] = 0.f;
+        fsum[acc_im(c, ld >> 1)] = 0.f;
+      }
+    }
+    __syncthreads();
     cur ^= 1;
   }
-  // last diagonal element after the final pending update
-  const int last = n - 1;
-  if (rank == last % G && tid == 0) {
-    float2 a = Ak[(size_t)last * ld + last];
-    if (pend) {
-      const float2* vP = DET ? trd_sm + (size_t)(1 - cur) * ld : trd_sm + (size_t)(2 * (1 - cur)) * ld;
-      const float2* wP = DET ? trd_sm + 2 * (size_t)ld : trd_sm + (size_t)(2 * (1 - cur) + 1) * ld;
-      const float2 t1 = cmul(vP[last], conjf2(wP[last])), t2 = cmul(wP[last], conjf2(vP[last]));
-      a.x -= t1.x + t2.x;
+  // last diagonal element: A_s(n-1, n-1) - 2 Re sum_u V(n-1, u) conj W(n-1, u)
+  if (p1 == n - 1 && rank == (n - 1) % G && warp == 0) {
+    float s = 0.f;
+    if (lane < a.nbp) {
+      const float2 xv = XHk[(size_t)(n - 1) * kTrdXW + lane], xw = XHk[(size_t)(n - 1) * kTrdXW + kTrdNb + lane];
+      s = xv.x * xw.x + xv.y * xw.y;
     }
-    dout[(size_t)k * n + last] = a.x;
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) a.d[(size_t)k * n + n - 1] = Ak[(size_t)(n - 1) * ld + n - 1].x - 2.f * s;
   }
   cl.sync();
 }
-
 // ---------------------------------------------------------------------------
 // 3. tridiagonal eigen-solve
 // ---------------------------------------------------------------------------
@@ -627,15 +814,16 @@ __global__ void invit_kernel(const double* __restrict__ d, const double* __restr
 
 // Modified Gram-Schmidt (twice) inside every group of consecutive
 // eigenvalues closer than tol * max|lambda|: inverse iteration cannot separate
-// those, any orthonormal basis of their span serves.  One CTA per k; thread 0
-// lists the groups, one warp per group.  Writes the result as complex FP32
-// columns into Zc [nk][n][n].
+// those, any orthonormal basis of their span serves.  Grid (nk, kMgsCtas):
+// thread 0 of every CTA lists the k's groups, warp w of CTA c takes groups
+// w + 8 c, w + 8 c + 8 kMgsCtas, ...
+constexpr int kMgsCtas = 16;
 __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict__ lam,
-                                                        double* __restrict__ Z, int n, int ld, double tol,
-                                                        float2* __restrict__ Zc) {
+                                                        double* __restrict__ Z, int n, double tol) {
   extern __shared__ int gstart[];
   __shared__ int ng;
-  const int k = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+  const int gw = blockIdx.y * (blockDim.x >> 5) + (tid >> 5), nw = gridDim.y * (blockDim.x >> 5);
   const double* lk = lam + (size_t)k * n;
   if (tid == 0) {
     double amax = 0.0;
@@ -652,7 +840,7 @@ __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict
   }
   __syncthreads();
   double* Zk = Z + (size_t)k * n * n;
-  for (int g = warp; g < ng; g += blockDim.x >> 5) {
+  for (int g = gw; g < ng; g += nw) {
     const int s0 = gstart[2 * g], s1 = gstart[2 * g + 1];
     for (int m = s0 + 1; m < s1; ++m) {
       double* zm = Zk + (size_t)m * n;
@@ -674,11 +862,16 @@ __global__ void __launch_bounds__(256) group_mgs_kernel(const double* __restrict
       }
     }
   }
-  __syncthreads();
-  float2* Zck = Zc + (size_t)k * n * ld;
-  for (size_t e = tid; e < (size_t)n * ld; e += blockDim.x) {
-    const int r = (int)(e % ld), c = (int)(e / ld);
-    Zck[e] = make_float2(r < n ? (float)Zk[(size_t)c * n + r] : 0.f, 0.f);
+}
+
+// The tridiagonal eigenvectors as complex FP32 columns of even length
+// (Zc [nk][n][ld], a zero padding row for odd n).
+__global__ void z_to_c32_kernel(const double* __restrict__ Z, int n, int ld, int nk, float2* __restrict__ Zc) {
+  const size_t total = (size_t)nk * n * ld;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e % ld);
+    const size_t kc = e / ld;          // k * n + column
+    Zc[e] = make_float2(r < n ? (float)Z[kc * n + r] : 0.f, 0.f);
   }
 }
 
@@ -752,18 +945,40 @@ static int max_smem_optin() {
   return smem;
 }
 
-int hetrd_max_n() { return (max_smem_optin() - 2048) / (4 * (int)sizeof(float2)); }
+// Static shared memory of a panel kernel variant.
+static size_t trd_static_smem(bool det) {
+  cudaFuncAttributes fa{};
+  if ((det ? cudaFuncGetAttributes(&fa, hetrd_panel_kernel<true>)
+           : cudaFuncGetAttributes(&fa, hetrd_panel_kernel<false>)) != cudaSuccess) {
+    cudaGetLastError();
+    return 32768;
+  }
+  return fa.sharedSizeBytes;
+}
 
-// Shared memory of the tridiagonalisation: 32 (float) or 40 (DET) bytes per row.
-static size_t hetrd_smem(int ld, bool det) { return (det ? 40 : 32) * (size_t)ld; }
+// Dynamic shared memory of the panel kernel: the two column buffers and the
+// partial products, 32 (DET) or 24 (float) bytes per row.
+static size_t hetrd_smem(int ld, bool det) { return (det ? 32 : 24) * (size_t)ld; }
 
-// The deterministic variant wherever its shared memory fits.
-static bool hetrd_det(int ld) { return hetrd_smem(ld, true) + 2048 <= (size_t)max_smem_optin(); }
+// The deterministic variant up to n = kTrdDetMaxN (where its shared memory
+// fits too); above, the FP32-atomic variant, whose half-width atomics stream
+// the large matrices faster (Si512: 1.86 against 2.27 s per pass).
+// OLC_TRD_DET=0 / 1 selects a variant wherever it fits.
+constexpr int kTrdDetMaxN = 4096;
+static bool hetrd_det(int ld) {
+  bool want = ld <= kTrdDetMaxN;
+  if (const char* v = std::getenv("OLC_TRD_DET")) want = v[0] != '0';
+  if (!want) return false;
+  return hetrd_smem(ld, true) + trd_static_smem(true) <= (size_t)max_smem_optin();
+}
 
-// One tridiagonalisation launch with clusters of G CTAs (one cluster per k);
-// G = 16 is a non-portable cluster size (allowed explicitly).
-static int launch_hetrd(olc_context* ctx, int G, float2* H, int n, int ld, int nk, size_t smem, double* d,
-                        double* e, float2* tau) {
+int hetrd_max_n() {
+  return (int)(((size_t)max_smem_optin() - trd_static_smem(false)) / 24) & ~1;
+}
+
+// One panel launch with clusters of G CTAs (one cluster per k); G = 16 is a
+// non-portable cluster size (allowed explicitly).
+static int launch_panel(olc_context* ctx, int G, const TrdArgs& args, int nk, size_t smem, bool det) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(G, nk, 1);
   cfg.blockDim = dim3(kTrdThreads, 1, 1);
@@ -776,14 +991,14 @@ static int launch_hetrd(olc_context* ctx, int G, float2* H, int n, int ld, int n
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (hetrd_det(ld))
-    return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel<true>, H, n, ld, d, e, tau), "hetrd launch");
-  return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_kernel<false>, H, n, ld, d, e, tau), "hetrd launch");
+  if (det) return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_panel_kernel<true>, args), "hetrd panel launch");
+  return cuda_check(cudaLaunchKernelEx(&cfg, hetrd_panel_kernel<false>, args), "hetrd panel launch");
 }
 
-// Whether clusters of G CTAs of this kernel with this shared memory can be
-// resident at all (16 exceeds the portable limit and may not fit a GPC).
-static bool cluster_fits(int G, int ld, size_t smem) {
+// How many clusters of G CTAs of the panel kernel with this shared memory can
+// be resident at once (0: none; 16 exceeds the portable limit and may not fit
+// a GPC).
+static int max_clusters(int G, size_t smem, bool det) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(G, 1, 1);
   cfg.blockDim = dim3(kTrdThreads, 1, 1);
@@ -796,27 +1011,68 @@ static bool cluster_fits(int G, int ld, size_t smem) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int nclusters = 0;
-  const cudaError_t r = hetrd_det(ld) ? cudaOccupancyMaxActiveClusters(&nclusters, hetrd_kernel<true>, &cfg)
-                                      : cudaOccupancyMaxActiveClusters(&nclusters, hetrd_kernel<false>, &cfg);
+  const cudaError_t r = det ? cudaOccupancyMaxActiveClusters(&nclusters, hetrd_panel_kernel<true>, &cfg)
+                            : cudaOccupancyMaxActiveClusters(&nclusters, hetrd_panel_kernel<false>, &cfg);
   if (r != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return 0;
   }
-  return nclusters > 0;
+  return nclusters;
+}
+
+// The whole reduction: a panel launch per kTrdNb reflectors, the trailing
+// update A22 -= [V W] [W V]^H between panels (lower tiles only; the panel
+// kernel reads nothing above the diagonal).  first_only: the first panel
+// alone (the tuner's sample).
+static int hetrd_run(olc_context* ctx, int G, float2* H, int n, int ld, int nk, size_t smem, bool det, double* d,
+                     double* e, float2* tau, float2* XH, float2* YH, double* fro, bool first_only) {
+  const long long sX = 2LL * n * kTrdXW;          // floats per k of XH, YH
+  for (int p0 = 0; p0 < n - 1; p0 += kTrdNb) {
+    const int nbp = std::min(kTrdNb, n - 1 - p0);
+    const TrdArgs args{H, XH, YH, d, e, tau, fro, n, ld, p0, nbp};
+    int st;
+    {
+      StageScope scope(ctx, OLC_STAGE_TRIDIAG, 1);
+      if ((st = launch_panel(ctx, G, args, nk, smem, det))) return st;
+    }
+    if (first_only) return OLC_OK;
+    const int p1 = p0 + nbp;
+    if (p1 < n - 1) {
+      const int m = n - p1;
+      const float* Xf = reinterpret_cast<const float*>(XH) + 2LL * p1 * kTrdXW;
+      const float* Yf = reinterpret_cast<const float*>(YH) + 2LL * p1 * kTrdXW;
+      float* C = reinterpret_cast<float*>(H) + 2 * ((size_t)p1 * ld + p1);
+      if ((st = tc::cgemm_f32(ctx, m, m, kTrdXW, Xf, sX, kTrdXW, true, Yf, sX, kTrdXW, -1.f, 1.f, C, 2LL * n * ld, ld,
+                              nk, OLC_STAGE_TRIDIAG, /*lower=*/true)))
+        return st;
+    }
+  }
+  return OLC_OK;
 }
 
 // Autotuner of the CTAs per k: the first pass of a context for a given
-// (n, nk) times every candidate cluster size that keeps the launch within two
-// waves, each on a copy of the reduced matrices, and keeps the fastest.
-static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk, size_t smem, double* d,
-                        double* e, float2* tau, int* G) {
+// (n, nk) times the first panel (the longest product of the reduction) with
+// every candidate cluster size that keeps the launch within two waves, on a
+// copy of the reduced matrices, and keeps the fastest.
+static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk, size_t smem, bool det, double* d,
+                        double* e, float2* tau, float2* XH, float2* YH, double* fro, int* G) {
   if (ctx->trd_tuned_n == n && ctx->trd_tuned_nk == nk) {
     *G = ctx->trd_tuned_g;
     return OLC_OK;
   }
-  int cand[5], nc = 0;
-  for (int g = 1; g <= 16; g *= 2)
-    if (g * nk <= 2 * 152 && (g * nk >= 38 || g == 8) && cluster_fits(g, ld, smem)) cand[nc++] = g;
+  // candidates: the powers of two within two waves, and the largest cluster
+  // size whose nk clusters are all resident at once (one wave, which need
+  // not be a power of two: a 16-CTA cluster takes a whole GPC)
+  int cand[6], nc = 0;
+  for (int g = 1; g <= kTrdMaxG; g *= 2)
+    if (g * nk <= 2 * 152 && (g * nk >= 38 || g == 8) && max_clusters(g, smem, det) > 0) cand[nc++] = g;
+  for (int g = kTrdMaxG; g > 1; --g)
+    if (max_clusters(g, smem, det) >= nk) {
+      bool have = false;
+      for (int j = 0; j < nc; ++j) have |= cand[j] == g;
+      if (!have) cand[nc++] = g;
+      break;
+    }
   if (!nc) cand[nc++] = 1;
   int best = cand[0];
   if (nc > 1) {
@@ -831,12 +1087,11 @@ static int tune_cluster(olc_context* ctx, const float2* H, int n, int ld, int nk
     for (int i = 0; i < nc; ++i) {
       cudaMemcpyAsync(scratch, H, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
       cudaEventRecord(a, ctx->stream);
-      st = launch_hetrd(ctx, cand[i], scratch, n, ld, nk, smem, d, e, tau);
+      st = hetrd_run(ctx, cand[i], scratch, n, ld, nk, smem, det, d, e, tau, XH, YH, fro, true);
       cudaEventRecord(b, ctx->stream);
       if (!st) st = cuda_check(cudaEventSynchronize(b), "tuning sync");
       float ms = 0.f;
       cudaEventElapsedTime(&ms, a, b);
-      count_launch();
       if (st) break;
       if (ms < best_ms) { best_ms = ms; best = cand[i]; }
     }
@@ -947,24 +1202,35 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, const float* h32, const 
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&e, 8ULL * (n - 1) * nk, stream), "malloc e"))) return st;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&tau, 8ULL * (n - 1) * nk, stream), "malloc tau"))) return st;
   {
-    StageScope scope(ctx, OLC_STAGE_TRIDIAG, 1);
-    // streamed traffic: the trailing lower triangle read and written at every step
-    add_work(ctx, OLC_STAGE_TRIDIAG, 0.0, 8.0 * ((double)n * n * n - n) / 3.0 * nk);
+    // algorithmic traffic: every step reads the trailing lower triangle once;
+    // every trailing update reads and writes the lower triangle it changes
+    double bytes = 8.0 * ((double)n * n * n - n) / 6.0;
+    for (int p1 = kTrdNb; p1 < n - 1; p1 += kTrdNb) bytes += 16.0 * (double)(n - p1) * (n - p1 + 1) / 2.0;
+    add_work(ctx, OLC_STAGE_TRIDIAG, 0.0, bytes * nk);
     const bool det = hetrd_det(ld);
     const size_t smem = hetrd_smem(ld, det);
-    if ((st = cuda_check(cudaFuncSetAttribute(det ? hetrd_kernel<true> : hetrd_kernel<false>,
+    if ((st = cuda_check(cudaFuncSetAttribute(det ? hetrd_panel_kernel<true> : hetrd_panel_kernel<false>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                          "hetrd smem"))) return st;
-    if ((st = cuda_check(cudaFuncSetAttribute(det ? hetrd_kernel<true> : hetrd_kernel<false>,
+    if ((st = cuda_check(cudaFuncSetAttribute(det ? hetrd_panel_kernel<true> : hetrd_panel_kernel<false>,
                                               cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
                          "hetrd cluster size"))) return st;
+    float2 *XH = nullptr, *YH = nullptr;
+    double* fro = nullptr;
+    const size_t xbytes = sizeof(float2) * (size_t)kTrdXW * n * nk;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&XH, xbytes, stream), "malloc XH"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&YH, xbytes, stream), "malloc YH"))) return st;
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&fro, 8ULL * nk, stream), "malloc fro"))) return st;
     int G = 0;
     if (const char* v = std::getenv("OLC_TRD_CLUSTER")) {
       const int g = std::atoi(v);
-      if (g == 1 || g == 2 || g == 4 || g == 8 || g == 16) G = g;
+      if (g >= 1 && g <= kTrdMaxG) G = g;
     }
-    if (!G && (st = tune_cluster(ctx, H, n, ld, nk, smem, d, e, tau, &G))) return st;
-    if ((st = launch_hetrd(ctx, G, H, n, ld, nk, smem, d, e, tau))) return st;
+    if (!G && (st = tune_cluster(ctx, H, n, ld, nk, smem, det, d, e, tau, XH, YH, fro, &G))) return st;
+    if ((st = hetrd_run(ctx, G, H, n, ld, nk, smem, det, d, e, tau, XH, YH, fro, false))) return st;
+    cudaFreeAsync(XH, stream);
+    cudaFreeAsync(YH, stream);
+    cudaFreeAsync(fro, stream);
   }
   // ---- 3. tridiagonal eigen-solve -------------------------------------------
   const size_t TT = (size_t)n * nk;
@@ -983,7 +1249,9 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, const float* h32, const 
     const size_t gsm = sizeof(int) * 2 * (size_t)(n / 2 + 1);
     if ((st = cuda_check(cudaFuncSetAttribute(group_mgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)gsm), "mgs smem"))) return st;
-    group_mgs_kernel<<<nk, 256, gsm, stream>>>(lam, Z, n, ld, 1e-5, Xc);
+    group_mgs_kernel<<<dim3(nk, kMgsCtas), 256, gsm, stream>>>(lam, Z, n, 1e-5);
+    z_to_c32_kernel<<<152 * 16, 256, 0, stream>>>(Z, n, ld, nk, Xc);
+    scope.add_launches(1);
   }
   cudaFreeAsync(work, stream);
   cudaFreeAsync(piv, stream);
