@@ -545,12 +545,12 @@ __global__ void cluster_solve_kernel(const double* __restrict__ Hh, const float*
   }
 }
 
-// Final ascending order over all clusters; gathers eigenvalues and vectors.
+// Final ascending order over all clusters (one CTA per k): the eigenvalues,
+// and the slot of each output column in perm [nk][n] for gather_vectors_kernel.
 __global__ void __launch_bounds__(1024) final_sort_kernel(const double* __restrict__ w_slot,
-                                                          const double* __restrict__ v_slot,
                                                           int n, int num_states,
                                                           double* __restrict__ eig,
-                                                          double* __restrict__ vec) {
+                                                          int* __restrict__ perm) {
   extern __shared__ double sortmem[];
   int P0 = 1;
   while (P0 < n) P0 <<= 1;
@@ -578,15 +578,21 @@ __global__ void __launch_bounds__(1024) final_sort_kernel(const double* __restri
       }
       __syncthreads();
     }
-  for (int i = tid; i < num_states; i += blockDim.x) eig[(size_t)k * num_states + i] = key[i];
-  if (!vec) return;
-  const size_t nn = (size_t)n * n;
-  for (size_t e = tid; e < (size_t)n * num_states; e += blockDim.x) {
-    const int row = (int)(e % n), col = (int)(e / n);
-    const double* src = v_slot + 2 * ((size_t)k * nn + (size_t)idx[col] * n + row);
-    double* dst = vec + 2 * ((size_t)k * n * num_states + e);
-    dst[0] = src[0];
-    dst[1] = src[1];
+  for (int i = tid; i < num_states; i += blockDim.x) {
+    eig[(size_t)k * num_states + i] = key[i];
+    perm[(size_t)k * n + i] = idx[i];
+  }
+}
+
+// Eigenvectors in the sorted order, every k at once (grid-stride over
+// [nk][num_states][n] complex).
+__global__ void gather_vectors_kernel(const double2* __restrict__ v_slot, const int* __restrict__ perm, int n,
+                                      int num_states, int nk, double2* __restrict__ vec) {
+  const size_t per = (size_t)n * num_states, total = per * nk;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = e / per, r = e % per;
+    const int row = (int)(r % n), col = (int)(r / n);
+    vec[e] = v_slot[(k * n + (size_t)perm[k * n + col]) * n + row];
   }
 }
 
@@ -909,7 +915,13 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     int P = 1;
     while (P < n) P <<= 1;
     const size_t sortmem = (size_t)P * (sizeof(double) + sizeof(int));
-    final_sort_kernel<<<nk, 1024, sortmem, stream>>>(w_slot, v_slot, n, num_states, eig_dev, vectors);
+    // L.order is free once the clusters are solved: it takes the permutation
+    final_sort_kernel<<<nk, 1024, sortmem, stream>>>(w_slot, n, num_states, eig_dev, L.order);
+    if (vectors) {
+      gather_vectors_kernel<<<152 * 16, 256, 0, stream>>>(reinterpret_cast<const double2*>(v_slot), L.order, n,
+                                                          num_states, nk, reinterpret_cast<double2*>(vectors));
+      scope.add_launches(1);
+    }
   }
   st = cuda_check(cudaGetLastError(), "final sort");
   cudaFreeAsync(L.order, stream);

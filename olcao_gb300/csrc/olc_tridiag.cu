@@ -167,34 +167,36 @@ __device__ __forceinline__ void acc_add(const TrdAcc& a, int c, float x, float y
   }
 }
 
-// One row pair (2q, 2q+1) of a set of owned columns, the matrix values
-// already loaded: the columns' products and the pair's mirrored products.
-// MASK: the pair may lie on or above a column's diagonal.
+// One row pair (2q, 2q+1) of a set of owned columns cb + t G (t < kTrdPanel;
+// a column >= n is an empty slot), the matrix values already loaded: the
+// columns' products and the pair's mirrored products.  MASK: the pair may lie
+// on or above a column's diagonal.
 template <bool DET, bool MASK>
-__device__ __forceinline__ void trd_pair(const float4 (&a4)[kTrdPanel], int n, int q, const int (&cr)[kTrdPanel],
+__device__ __forceinline__ void trd_pair(const float4 (&a4)[kTrdPanel], int n, int q, int cb, int G,
                                          const float2 (&vr)[kTrdPanel], float (&ax)[kTrdPanel],
                                          float (&ay)[kTrdPanel], const float4 vc, const TrdAcc& acc) {
   const int c0 = 2 * q;
   float s0x = 0.f, s0y = 0.f, s1x = 0.f, s1y = 0.f;
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
-    if (cr[t] >= n || (MASK && cr[t] > c0 + 1)) continue;
+    const int c = cb + t * G;
+    if (c >= n || (MASK && c > c0 + 1)) continue;
     float2 a0 = make_float2(a4[t].x, a4[t].y), a1 = make_float2(a4[t].z, a4[t].w);
     if (MASK) {                     // the diagonal is real
-      if (c0 == cr[t]) a0.y = 0.f;
-      if (c0 + 1 == cr[t]) a1.y = 0.f;
+      if (c0 == c) a0.y = 0.f;
+      if (c0 + 1 == c) a1.y = 0.f;
     }
-    if (!MASK || c0 >= cr[t]) {
+    if (!MASK || c0 >= c) {
       ax[t] += a0.x * vc.x + a0.y * vc.y;         // conj(a) v
       ay[t] += a0.x * vc.y - a0.y * vc.x;
     }
     ax[t] += a1.x * vc.z + a1.y * vc.w;
     ay[t] += a1.x * vc.w - a1.y * vc.z;
-    if (!MASK || c0 > cr[t]) {
+    if (!MASK || c0 > c) {
       s0x += a0.x * vr[t].x - a0.y * vr[t].y;
       s0y += a0.x * vr[t].y + a0.y * vr[t].x;
     }
-    if (!MASK || c0 + 1 > cr[t]) {
+    if (!MASK || c0 + 1 > c) {
       s1x += a1.x * vr[t].x - a1.y * vr[t].y;
       s1y += a1.x * vr[t].y + a1.y * vr[t].x;
     }
@@ -203,57 +205,58 @@ __device__ __forceinline__ void trd_pair(const float4 (&a4)[kTrdPanel], int n, i
   if (!MASK || s1x != 0.f || s1y != 0.f) acc_add<DET>(acc, c0 + 1, s1x, s1y);
 }
 
-// One set of kTrdPanel owned columns (slots past the last column are empty):
-// the pairs touching the diagonals first, then the bulk unmasked with two
-// pairs per lane in flight.  A_s is read through the non-coherent path: the
-// kernel writes only column i, which no product reads.
+// One set of kTrdPanel owned columns cb + t G (slots past the last column are
+// empty): the pairs touching the diagonals first, then the bulk unmasked
+// with two pairs per lane in flight.  A_s is read through the non-coherent
+// path: the kernel writes only column i, which no product reads.  Column
+// indices and offsets are formed from cb and G where they are used, which
+// keeps the loads of both pairs in registers.
 template <bool DET>
-__device__ __forceinline__ void trd_columns(const float2* __restrict__ Ak, int n, int ld, int r0, int G, int pn,
-                                            int nown, int lane, const float2* vC, const TrdAcc& acc) {
-  int cr[kTrdPanel];
+__device__ __noinline__ void trd_columns(const float2* __restrict__ Ak, int n, int ld, int r0, int G, int pn,
+                                            int lane, const float2* vC, const TrdAcc& acc) {
+  const int cb = r0 + pn * kTrdPanel * G;       // first column of the set
   float2 vr[kTrdPanel];
   float ax[kTrdPanel], ay[kTrdPanel];
-  int off[kTrdPanel];                           // column offsets in float4 units
-  int c_last = 0;
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
-    const int j = pn * kTrdPanel + t;
-    cr[t] = j < nown ? r0 + j * G : n;          // n marks an empty slot
-    const int rr = min(cr[t], n - 1);
-    if (cr[t] < n) c_last = cr[t];
-    vr[t] = vC[rr];
+    vr[t] = vC[min(cb + t * G, n - 1)];
     ax[t] = 0.f;
     ay[t] = 0.f;
-    off[t] = rr * (ld >> 1);
   }
-  const float4* A4 = reinterpret_cast<const float4*>(Ak);
+  const int h = ld >> 1;                        // float4 per column
+  const float4* A4 = reinterpret_cast<const float4*>(Ak) + (size_t)cb * h;
+  const int hs = G * h;                         // float4 between the set's columns
   const float4* vC4 = reinterpret_cast<const float4*>(vC);
-  const int q1 = ld >> 1;                       // the last pair may hold the zero padding row
+  const int c_last = min(cb + (kTrdPanel - 1) * G, n - 1 - (n - 1 - cb) % G);
+  const int q1 = h;                             // the last pair may hold the zero padding row
   const int qd = min(q1, (c_last >> 1) + 1);    // pairs from qd on lie below every diagonal
-  int q = (cr[0] >> 1) + lane;
+  int q = (cb >> 1) + lane;
   for (; q < qd; q += 32) {
     float4 a4[kTrdPanel];
 #pragma unroll
-    for (int t = 0; t < kTrdPanel; ++t)
-      a4[t] = (cr[t] < n && cr[t] <= 2 * q + 1) ? __ldg(A4 + off[t] + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-    trd_pair<DET, true>(a4, n, q, cr, vr, ax, ay, vC4[q], acc);
+    for (int t = 0; t < kTrdPanel; ++t) {
+      const int c = cb + t * G;
+      a4[t] = (c < n && c <= 2 * q + 1) ? __ldg(A4 + (size_t)t * hs + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    trd_pair<DET, true>(a4, n, q, cb, G, vr, ax, ay, vC4[q], acc);
   }
-  // the pairs below every diagonal: two pairs per lane in flight
   for (; q + 32 < q1; q += 64) {
     float4 a4[kTrdPanel], b4[kTrdPanel];
 #pragma unroll
     for (int t = 0; t < kTrdPanel; ++t) {
-      a4[t] = cr[t] < n ? __ldg(A4 + off[t] + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-      b4[t] = cr[t] < n ? __ldg(A4 + off[t] + q + 32) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const bool ok = cb + t * G < n;
+      a4[t] = ok ? __ldg(A4 + (size_t)t * hs + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+      b4[t] = ok ? __ldg(A4 + (size_t)t * hs + q + 32) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    trd_pair<DET, false>(a4, n, q, cr, vr, ax, ay, vC4[q], acc);
-    trd_pair<DET, false>(b4, n, q + 32, cr, vr, ax, ay, vC4[q + 32], acc);
+    trd_pair<DET, false>(a4, n, q, cb, G, vr, ax, ay, vC4[q], acc);
+    trd_pair<DET, false>(b4, n, q + 32, cb, G, vr, ax, ay, vC4[q + 32], acc);
   }
   if (q < q1) {
     float4 a4[kTrdPanel];
 #pragma unroll
-    for (int t = 0; t < kTrdPanel; ++t) a4[t] = cr[t] < n ? __ldg(A4 + off[t] + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-    trd_pair<DET, false>(a4, n, q, cr, vr, ax, ay, vC4[q], acc);
+    for (int t = 0; t < kTrdPanel; ++t)
+      a4[t] = cb + t * G < n ? __ldg(A4 + (size_t)t * hs + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    trd_pair<DET, false>(a4, n, q, cb, G, vr, ax, ay, vC4[q], acc);
   }
 #pragma unroll
   for (int t = 0; t < kTrdPanel; ++t) {
@@ -262,7 +265,7 @@ __device__ __forceinline__ void trd_columns(const float2* __restrict__ Ak, int n
       x += __shfl_xor_sync(0xffffffffu, x, o);
       y += __shfl_xor_sync(0xffffffffu, y, o);
     }
-    if (lane == 0 && cr[t] < n) acc_add<DET>(acc, cr[t], x, y);
+    if (lane == 0 && cb + t * G < n) acc_add<DET>(acc, cb + t * G, x, y);
   }
 }
 
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(kTrdThreads, 1) hetrd_panel_kernel(const __gri
       const TrdAcc acc{fsum, qsum, DET ? s_qscale : 1.f, ld >> 1};
       const int nown = r0 < n ? (n - r0 + G - 1) / G : 0;
       const int npanel = (nown + kTrdPanel - 1) / kTrdPanel;
-      for (int pn = warp; pn < npanel; pn += kTrdWarps) trd_columns<DET>(Ak, n, ld, r0, G, pn, nown, lane, vC, acc);
+      for (int pn = warp; pn < npanel; pn += kTrdWarps) trd_columns<DET>(Ak, n, ld, r0, G, pn, lane, vC, acc);
     }
     {
       // this CTA's share of XH^T v over its rows r > i: warp w takes columns 4w..4w+3
