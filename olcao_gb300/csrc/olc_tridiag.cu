@@ -186,19 +186,20 @@ __device__ __forceinline__ void trd_pair(const float4 (&a4)[kTrdPanel], int n, i
       if (c0 == c) a0.y = 0.f;
       if (c0 + 1 == c) a1.y = 0.f;
     }
+    // complex multiply-adds as chains of two fused multiply-adds each
     if (!MASK || c0 >= c) {
-      ax[t] += a0.x * vc.x + a0.y * vc.y;         // conj(a) v
-      ay[t] += a0.x * vc.y - a0.y * vc.x;
+      ax[t] = fmaf(a0.x, vc.x, fmaf(a0.y, vc.y, ax[t]));     // conj(a) v
+      ay[t] = fmaf(a0.x, vc.y, fmaf(-a0.y, vc.x, ay[t]));
     }
-    ax[t] += a1.x * vc.z + a1.y * vc.w;
-    ay[t] += a1.x * vc.w - a1.y * vc.z;
+    ax[t] = fmaf(a1.x, vc.z, fmaf(a1.y, vc.w, ax[t]));
+    ay[t] = fmaf(a1.x, vc.w, fmaf(-a1.y, vc.z, ay[t]));
     if (!MASK || c0 > c) {
-      s0x += a0.x * vr[t].x - a0.y * vr[t].y;
-      s0y += a0.x * vr[t].y + a0.y * vr[t].x;
+      s0x = fmaf(a0.x, vr[t].x, fmaf(-a0.y, vr[t].y, s0x));
+      s0y = fmaf(a0.x, vr[t].y, fmaf(a0.y, vr[t].x, s0y));
     }
     if (!MASK || c0 + 1 > c) {
-      s1x += a1.x * vr[t].x - a1.y * vr[t].y;
-      s1y += a1.x * vr[t].y + a1.y * vr[t].x;
+      s1x = fmaf(a1.x, vr[t].x, fmaf(-a1.y, vr[t].y, s1x));
+      s1y = fmaf(a1.x, vr[t].y, fmaf(a1.y, vr[t].x, s1y));
     }
   }
   if (!MASK || s0x != 0.f || s0y != 0.f) acc_add<DET>(acc, c0, s0x, s0y);
