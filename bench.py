@@ -46,7 +46,10 @@ WORKLOADS = {
     "graphite": "AB graphite 4 atoms, valence only, 32 basis fns, 8192 k (32x32x8 MP)",
     "quartz": "alpha-quartz SiO2 3x3x3 (243 atoms), 3159 basis fns (567 core), 9 k (Gamma + 2x2x2)",
     "si512": "Si512 4x4x4 diamond supercell, 6656 basis fns (2560 core), 9 k (Gamma + shifted 2x2x2)",
+    "batched": "uneven batch: AB graphite (n = 32, 8192 k) and Si8 (n = 104, 512 k), "
+               "one mixed pass of each per step (two passes back to back, not one launch)",
 }
+BATCHED_PARTS = ("graphite", "si8")
 
 
 def parse():
@@ -218,20 +221,41 @@ def one_thread_zhegv(n):
 def run_reference(args, world, rank):
     """CPU restatement of the iteration (oracle port): per k, H(k) assembled
     from the packed operators (readPackedMatrixAccum) and LAPACK zhegv
-    (solveZHEGV), on a bounded sample of the workload."""
+    (solveZHEGV), on a bounded sample of the workload.  The batched workload
+    sums the two systems' scaled samples."""
     if rank != 0:
         return
+    if args.config != "batched":
+        print(json.dumps(reference_line(args, world, args.config)), flush=True)
+        return
+    lines = [reference_line(args, world, name) for name in BATCHED_PARTS]
+    v = sum(l["value"] for l in lines)
+    line = dict(lines[0])
+    line.update({"value": v, "ms_per_step": v * 1e3, "value_from": "sum of the parts' scaled samples",
+                 "steps": min(l["steps"] for l in lines),
+                 "data": "synthetic seeded (graphite, si8)",
+                 "config": {"workload": WORKLOADS["batched"], "form": "stored", "precision": "fp64"},
+                 "cpu_baseline": {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                                  "sample": "; ".join(f"{n}: {l['cpu_baseline']['sample']}"
+                                                      for n, l in zip(BATCHED_PARTS, lines))},
+                 "one_thread": None, "k_solves_per_s": (8192 + 512) / v,
+                 "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    print(json.dumps(line), flush=True)
+
+
+def reference_line(args, world, config):
+    """The reference arm's JSON line for one workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     from olcao_gb300 import system as S
-    full = S.SYSTEMS[args.config]()
+    full = S.SYSTEMS[config]()
     nk, n, pd = full.num_kpoints, full.vale_dim, full.pot_dim
     t0 = time.perf_counter()
     if n <= CPU_SAMPLE_N:
         # real pencils: the oracle's packed operators of sampled k-points
         ns = max(1, min(args.cpu_sample_k, nk))
         idx = np.linspace(0, nk - 1, ns).round().astype(int)
-        part = S.SYSTEMS[args.config]()
+        part = S.SYSTEMS[config]()
         part.kpoints_abc = full.kpoints_abc[idx]
         o = orc.Oracle(part)
         packed = o.packed_operators()
@@ -285,7 +309,7 @@ def run_reference(args, world, rank):
             "steps_requested": args.steps, "warmup_requested": args.warmup,
             "higher_is_better": False, "scaling": "strong",
             "vs_baseline": None, "dtype": "fp64", "data": f"synthetic seeded ({full.name})",
-            "config": {"workload": WORKLOADS[args.config], "form": "stored",
+            "config": {"workload": WORKLOADS[config], "form": "stored",
                        "precision": "fp64"},
             "cpu_baseline": {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
@@ -293,7 +317,89 @@ def run_reference(args, world, rank):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "t_setup_s_sample": t_setup}
+    return line
+
+
+# ---------------------------------------------------------------------------
+def run_batched(args):
+    """The uneven batch: a mixed pass over graphite's 8192 k (n = 32, the
+    in-shared-memory batched solver) and one over Si8's 512 k (n = 104, the
+    batched FP32 solver and Rayleigh-Ritz) per step, each replayed as a CUDA
+    graph.  Reports s per step and k-point solves per second."""
+    import torch
+    from olcao_gb300 import api, build
+    from olcao_gb300 import system as S
+    if not os.path.exists(api.LIB_PATH):
+        build.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    parts = []
+    for name in BATCHED_PARTS:
+        sysm = S.SYSTEMS[name]()
+        ctx = api.Context(sysm)
+        ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+        cs = [sysm.pot_coeffs * (1.0 + 0.01 * ((s % 5) - 2)) for s in range(5)]
+        parts.append({"name": name, "ctx": ctx, "coeffs": cs,
+                      "dco": [torch.from_numpy(c).cuda() for c in cs],
+                      "host": [torch.from_numpy(c).pin_memory() for c in cs],
+                      "eig": torch.empty(ctx.nk, ctx.vale_dim, dtype=torch.float64, device="cuda"),
+                      "eig_host": torch.empty(ctx.nk, ctx.vale_dim, dtype=torch.float64).pin_memory(),
+                      "vec": torch.empty(ctx.nk, ctx.vale_dim, ctx.vale_dim, dtype=torch.complex128,
+                                         device="cuda")})
+
+    def step(s, host=False):
+        for p in parts:
+            c = p["host"][s % 5].numpy() if host else p["dco"][s % 5]
+            out = p["eig_host"].numpy() if host else p["eig"]
+            p["ctx"].scf_iteration(c, p["ctx"].vale_dim, eig_out=out, vectors=p["vec"],
+                                   precision=api.PREC_MIXED, graph=True)
+
+    for w in range(args.warmup):
+        step(w)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = api.launch_count()
+    pr, fh = clocks_start()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for s in range(args.steps):
+        step(s)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clocks_stop(pr, fh)
+    launches = api.launch_count() - l0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    mixed = [p["eig"].cpu().numpy().copy() for p in parts]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 5))
+    for s in range(e2e_steps):
+        step(s, host=True)
+    torch.cuda.synchronize()
+    e2e = (time.perf_counter() - t0) / e2e_steps
+    acc = {}
+    last = (args.steps - 1) % 5
+    for p, wm in zip(parts, mixed):
+        w64 = p["ctx"].scf_iteration(p["dco"][last], p["ctx"].vale_dim, precision=api.PREC_FP64)
+        acc[p["name"]] = float(np.abs(wm - w64).max())
+    nk_total = sum(p["ctx"].nk for p in parts)
+    h2d = sum(p["host"][0].numel() * 8 for p in parts)
+    d2h = sum(p["eig_host"].numel() * 8 for p in parts)
+    line = {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "strong",
+            "vs_baseline": None, "dtype": "fp64+fp32+bf16", "data": "synthetic seeded (graphite, si8)",
+            "config": {"workload": WORKLOADS["batched"], "form": "stored", "precision": "mixed",
+                       "num_kpoints": nk_total, "cuda_graph": True},
+            "k_solves_per_s": nk_total / (ms / 1e3),
+            "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps},
+            "gpu_launches": int(launches),
+            "accuracy": {"max_abs_eig_err_ha": acc,
+                         "reference": "plain FP64 GPU path on the same H(k), S(k)"},
+            "roofline": None, "cpu_baseline": None, "clocks": clocks}
     print(json.dumps(line), flush=True)
+    for p in parts:
+        p["ctx"].close()
 
 
 # ---------------------------------------------------------------------------
@@ -577,6 +683,9 @@ def main():
         run_reference(args, world, rank)
     elif args.valence_rho_only:
         run_valence_rho_only(args)
+    elif args.config == "batched":
+        if rank == 0:
+            run_batched(args)
     else:
         run_ours(args, world, rank, dist)
     if dist:

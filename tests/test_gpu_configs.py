@@ -2,14 +2,20 @@
 
 * Diamond, 216 k-points (n = 8 or 10): every k against the oracle's
   storage-form H(k), S(k) and LAPACK zhegv, eigenvalues within 1e-8 Ha.
-* Graphite (n = 32, valence only) on a slice of its 32x32x8 mesh: GPU
-  integrals and batched small solver against the oracle on sampled k.
+* Graphite (n = 32, valence only) on a slice of its 32x32x8 mesh and on the
+  whole mesh (8192 k): GPU integrals and batched small solver against the
+  oracle on sampled k.
 * Si8 (n = 104) on its full 8x8x8 mesh: mixed path against the FP64 path
   (1e-6 Ha), FP64 path against the oracle on sampled k (1e-8 Ha).
 * Si8 full mesh solved 20 times in one process in mixed form: every run
   within 1e-6 Ha of the FP64 path and bit-identical to the first (the
   tridiagonalisation sums in fixed point, the cluster solves in a fixed
   order).
+* Si8 with a diffuse basis (alpha_min 0.06 and 0.04 instead of 0.12), whose
+  S(k) has condition numbers of 3e5 and 5e6 (min eig(S) 4e-5 and 4e-6, so
+  an FP32 Cholesky would keep no correct digit at the latter): the mixed
+  path, which factors S in FP64, still meets 1e-6 Ha against the FP64 path
+  at every k, and the FP64 path meets 1e-8 Ha against the oracle at Gamma.
 Properties that do not depend on size hold at every k: ascending order,
 S-orthonormal vectors.
 """
@@ -60,6 +66,58 @@ def test_graphite_mesh_slice_matches_oracle(gpu_lib):
     ref = _oracle_eigs(sysm, kidx)
     assert np.abs(w[kidx] - ref).max() <= EIG_TOL
     assert (np.diff(w, axis=1) >= 0).all()
+
+
+@pytest.mark.gpu
+def test_graphite_full_mesh_matches_oracle(gpu_lib):
+    from olcao_gb300 import api
+    sysm = S.SYSTEMS["graphite"]()
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n, nk = ctx.vale_dim, ctx.nk
+    assert n == 32 and nk == 8192
+    w = ctx.scf_iteration(sysm.pot_coeffs, n, precision=api.PREC_MIXED)
+    assert np.isfinite(w).all() and (np.diff(w, axis=1) >= 0).all()
+    kidx = np.array([0, 1234, 4095, 5000, nk - 1])
+    ref = _oracle_eigs(sysm, kidx)
+    assert np.abs(w[kidx] - ref).max() <= EIG_TOL
+
+
+def _si8_diffuse(amin, mesh=(2, 2, 2), seed=5):
+    """The Si8 cell (valence only, n = 104) with its 18 Gaussians spread from
+    amin instead of 0.12: the more diffuse tail makes S(k) ill-conditioned."""
+    rng = np.random.default_rng(seed)
+    a = 5.431 * S.ANGSTROM
+    frac8 = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0],
+                      [.25, .25, .25], [.25, .75, .75], [.75, .25, .75], [.75, .75, .25]])
+    vec, pos = S._supercell(a * np.eye(3), frac8, (1, 1, 1))
+    t = S.make_type(rng, 1, 18, amin, 1.0e6, (18, 18, 12, 0), (0, 1, 2, 0, 1), ())
+    return S._finish(f"si8-amin{amin}", vec, [t], [0] * 8, pos, [S.silicon_pot()], S.mp_mesh(mesh),
+                     rng, seed, pot_of_type={0: 0})
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("amin,smin_max", [(0.06, 1e-4), (0.04, 1e-5)])
+def test_ill_conditioned_overlap_mixed_meets_bar(gpu_lib, amin, smin_max):
+    from olcao_gb300 import api
+    sysm = _si8_diffuse(amin)
+    ctx = api.Context(sysm)
+    ctx.scf_prepare(api.PREC_FP64, api.FORM_STORED)
+    n, nk = ctx.vale_dim, ctx.nk
+    assert n == 104 and nk == 8
+    # the smallest eigenvalue of S(k) over the mesh (Gamma is the worst k)
+    ev = min((np.linalg.eigvalsh(ctx.scf_matrices(sysm.pot_coeffs, k)[1]) for k in range(nk)),
+             key=lambda e: e[0])
+    assert ev[0] < smin_max, f"min eig(S) {ev[0]:.2e}: the pencil is not ill-conditioned"
+    w64 = ctx.scf_iteration(sysm.pot_coeffs, n, precision=api.PREC_FP64)
+    wm = ctx.scf_iteration(sysm.pot_coeffs, n, precision=api.PREC_MIXED)
+    err = np.abs(wm - w64)
+    k, i = np.unravel_index(np.argmax(err), err.shape)
+    assert err.max() <= MIXED_EIG_TOL, (f"cond(S) {ev[-1] / ev[0]:.1e}, k {k} state {i}: "
+                                        f"mixed {wm[k, i]} fp64 {w64[k, i]}")
+    nocc = 16                                   # 4 valence electrons per Si, 2 per state
+    assert abs(2.0 * (wm[:, :nocc].sum() - w64[:, :nocc].sum()) / nk) <= 1e-5
+    assert np.abs(w64[:1] - _oracle_eigs(sysm, np.array([0]))).max() <= EIG_TOL
 
 
 @pytest.mark.gpu
