@@ -368,7 +368,9 @@ int olc_populate_states(int num_states, int num_kpoints, int spin, const double*
 /* Primitive-level entry (testing and integration checks): one call of the
  * generated primitives (gaussIntegrals.f90) for a batch of inputs on the
  * device.  kind: 1 overlap2CIntg, 2 kinetic2CIntg, 3 nuclear3CIntg,
- * 4 electron3CIntg, 5 massvel2CIntg.  in[n*12] = (a1,a2,a3,Ax,Ay,Az,Bx,By,Bz,Cx,Cy,Cz),
+ * 4 electron3CIntg, 5 massvel2CIntg, 6 / 7 / 8 the x / y / z component of
+ * momentum2CIntg (gaussIntegrals.f90:23041-39068, <a| d/dr |b>).
+ * in[n*12] = (a1,a2,a3,Ax,Ay,Az,Bx,By,Bz,Cx,Cy,Cz),
  * lmalpha[n*2]; out[n*256] = sh(16,16) column-major (host arrays). */
 int olc_primitive_batch(int kind, int n, const double* in,
                         const int32_t* lmalpha, double* out);

@@ -137,7 +137,8 @@ def launch_count() -> int:
 
 def primitive_batch(kind: int, params: np.ndarray, lmalpha: np.ndarray) -> np.ndarray:
     """Evaluate primitive sh(16,16) blocks on the device (kind 1 overlap,
-    2 kinetic, 3 nuclear, 4 electron 3-centre); returns [n, 16, 16] indexed
+    2 kinetic, 3 nuclear, 4 electron 3-centre, 5 mass velocity, 6 / 7 / 8
+    the x / y / z momentum component); returns [n, 16, 16] indexed
     [item, row lm1, col lm2]."""
     p = np.ascontiguousarray(params, np.float64)
     lm = np.ascontiguousarray(lmalpha, np.int32)

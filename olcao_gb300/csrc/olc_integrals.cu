@@ -306,7 +306,7 @@ __global__ void prim_batch_kernel(int kind, int n, const double* in, const int32
 
 int primitive_batch_device(int kind, int n, const double* in, const int32_t* lmalpha,
                            double* out) {
-  if (kind < 1 || kind > 5 || n < 0) return fail(OLC_ERR_ARG, "olc_primitive_batch: bad kind");
+  if (kind < 1 || kind > 8 || n < 0) return fail(OLC_ERR_ARG, "olc_primitive_batch: bad kind");
   for (int i = 0; i < n; ++i) {
     for (int s = 0; s < 2; ++s) {
       int l = lmalpha[2 * i + s];
@@ -332,7 +332,8 @@ int primitive_batch_device(int kind, int n, const double* in, const int32_t* lma
       case 2: launch_prim_batch_f_kinetic(n, din, dlm, dout); break;
       case 3: launch_prim_batch_f_nuclear(n, din, dlm, dout); break;
       case 4: launch_prim_batch_f_elecpot(n, din, dlm, dout); break;
-      default: launch_prim_batch_f_massvel(n, din, dlm, dout); break;
+      case 5: launch_prim_batch_f_massvel(n, din, dlm, dout); break;
+      default: launch_prim_batch_f_momentum(kind, n, din, dlm, dout); break;
     }
     count_launch(7);
     st = cuda_check(cudaGetLastError(), "prim_batch_kernel");

@@ -19,4 +19,10 @@ void launch_prim_batch_f_overlap(int n, const double* in, const int32_t* lm, dou
   launch_prim_batch_f_kind<1>(n, in, lm, out);
 }
 
+void launch_prim_batch_f_momentum(int kind, int n, const double* in, const int32_t* lm, double* out) {
+  if (kind == 6) launch_prim_batch_f_kind<6>(n, in, lm, out);
+  else if (kind == 7) launch_prim_batch_f_kind<7>(n, in, lm, out);
+  else launch_prim_batch_f_kind<8>(n, in, lm, out);
+}
+
 }  // namespace olc

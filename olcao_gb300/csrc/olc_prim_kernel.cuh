@@ -202,6 +202,7 @@ __device__ __forceinline__ void prim_one(int kind, const double* in, double* out
   else if (kind == 2) add_kinetic<L1, L2>(in[0], in[1], A, B, 1.0, cart);
   else if (kind == 3) add_nuclear<L1, L2>(in[0], in[1], in[2], A, B, C, 1.0, cart);
   else if (kind == 5) add_massvel<L1, L2>(in[0], in[1], A, B, 1.0, cart);
+  else if (kind >= 6) add_momentum<L1, L2>(in[0], in[1], A, B, kind - 6, 1.0, cart);
   else {
     double d2 = 0.0;
     for (int c = 0; c < 3; ++c) d2 += (A[c] - B[c]) * (A[c] - B[c]);
@@ -224,13 +225,14 @@ int launch_prim_f_nuclear(cudaStream_t st, const SysView& v, const PrimArgs& a, 
 int launch_prim_f_elecpot(cudaStream_t st, const SysView& v, const PrimArgs& a, int l1, int l2, int mode, dim3 g,
                           dim3 b);
 // primitive batch entries of the f classes, one per kind (1 overlap,
-// 2 kinetic, 3 nuclear, 4 three-centre, 5 mass velocity), in the same
-// translation units
+// 2 kinetic, 3 nuclear, 4 three-centre, 5 mass velocity, 6-8 momentum x, y,
+// z with the overlap), in the same translation units
 void launch_prim_batch_f_overlap(int n, const double* in, const int32_t* lm, double* out);
 void launch_prim_batch_f_kinetic(int n, const double* in, const int32_t* lm, double* out);
 void launch_prim_batch_f_nuclear(int n, const double* in, const int32_t* lm, double* out);
 void launch_prim_batch_f_elecpot(int n, const double* in, const int32_t* lm, double* out);
 void launch_prim_batch_f_massvel(int n, const double* in, const int32_t* lm, double* out);
+void launch_prim_batch_f_momentum(int kind, int n, const double* in, const int32_t* lm, double* out);
 
 // Primitive batch kernel of one kind and one f class (a kernel per class
 // keeps each recurrence's register allocation separate).

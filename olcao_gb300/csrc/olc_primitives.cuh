@@ -228,6 +228,46 @@ __device__ __forceinline__ double lap2d(const double (&s)[LI + 1][LJ + 5], int i
   if (j >= 2) v += j * (j - 1) * lap1d<LI, LJ>(s, i, j - 2, a2);
   return v;
 }
+
+// Momentum (momentum2CIntg): component `comp` of <a| d/dr_comp |b>, the
+// derivative acting on b: d/dx [x^l e^{-a2 x^2}] = (l x^{l-1} - 2 a2 x^{l+1})
+// e^{-a2 x^2}, a 1-D overlap with b's power lowered or raised by one in that
+// direction times the plain overlaps of the other two.
+template <int L1, int L2>
+__device__ __forceinline__ void add_momentum(double a1, double a2, const double* A, const double* B, int comp,
+                                             double w, double* cart) {
+  constexpr int N1 = ncart(L1), N2 = ncart(L2);
+  const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
+  double s[3][L1 + 1][L2 + 2];
+  double d2 = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double P = (a1 * A[c] + a2 * B[c]) / z;
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    os1d<L1, L2 + 1>(P - A[c], P - B[c], inv2z, s[c]);
+  }
+  const double r = kPi / z;
+  const double pref = w * r * sqrt(r) * exp(-xi * d2);
+#pragma unroll
+  for (int a = 0; a < N1; ++a)
+#pragma unroll
+    for (int b = 0; b < N2; ++b) {
+      double v = pref;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int ia = cexp(a, c), jb = cexp(b, c);
+        if (c == comp) {
+          double d = -2.0 * a2 * s[c][ia][jb + 1];
+          if (jb > 0) d += jb * s[c][ia][jb - 1];
+          v *= d;
+        } else {
+          v *= s[c][ia][jb];
+        }
+      }
+      cart[a * N2 + b] += v;
+    }
+}
+
 template <int L1, int L2>
 __device__ __forceinline__ void add_massvel(double a1, double a2, const double* A,
                                             const double* B, double w, double* cart) {

@@ -18,6 +18,7 @@ arithmetic and operation order:
 * ``electron3CIntg``  gaussIntegrals.f90:11624-16023
 * ``boys``            gaussIntegrals.f90:16080-16221
 * ``nuclear3CIntg``   gaussIntegrals.f90:16223-23039
+* ``momentum2CIntg``  gaussIntegrals.f90:23041-39068 (sh(16,16,3))
 
 Fortran typing rules that change results are honoured: a real literal with a
 ``d`` exponent is double precision, a real literal without one is a
@@ -38,7 +39,7 @@ import numpy as np
 PI = 3.141592653589793  # src/constants.f90:36
 
 _SUBROUTINES = ("overlap2CIntg", "kinetic2CIntg", "electron3CIntg",
-                "nuclear3CIntg", "massvel2CIntg", "boys")
+                "nuclear3CIntg", "massvel2CIntg", "momentum2CIntg", "boys")
 # fineStructure of src/constants.f90:47 (in units of 1e-3), the only
 # module constant besides pi that the generated integrals read
 FINE_STRUCTURE = 7.2973525693
@@ -259,13 +260,14 @@ class FortranIntegrals:
                     "electron3CIntg": "a1, a2, a3, a, b, c, l1l2switch",
                     "nuclear3CIntg": "a1, a2, a3, a, b, c, l1l2switch",
                     "massvel2CIntg": "a1, a2, a, b, l1l2switch",
+                    "momentum2CIntg": "a1, a2, a, b, l1l2switch",
                     "boys": "t"}[name]
             if name == "boys":
                 pre = "    s = {}\n    f = {}\n"
                 post = "\n    return [f[(m,)] for m in range(1, 8)]"
             else:
                 pre = ("    pc = {}\n    pc_ol = {}\n    pc_ke = {}\n    sh = {}\n"
-                       "    prefactorn = {}\n    f = {}\n")
+                       "    prefactorn = {}\n    prefactormm = {}\n    f = {}\n")
                 post = "\n    return sh"
             code = f"def _{name}({args}):\n{pre}{body}{post}\n"
             ns = {"_exp": _exp, "_sqrt": _sqrt, "_sum": _sum, "_erf": _erf,
@@ -307,6 +309,15 @@ class FortranIntegrals:
     def massvel(self, a1, a2, A, B, switch):
         return self._run("massvel2CIntg", float(a1), float(a2),
                          np.asarray(A, float), np.asarray(B, float), int(switch))
+
+    def momentum(self, a1, a2, A, B, switch):
+        """momentum2CIntg: sh(16,16,3), the x, y, z components."""
+        sh = self.__dict__["_fn_momentum2CIntg"](float(a1), float(a2), np.asarray(A, float),
+                                                   np.asarray(B, float), int(switch))
+        out = np.full((16, 16, 3), np.nan)
+        for (i, j, c), v in sh.items():
+            out[i - 1, j - 1, c - 1] = v
+        return out
 
     def electron3c(self, a1, a2, a3, A, B, C, switch):
         return self._run("electron3CIntg", float(a1), float(a2), float(a3),

@@ -250,6 +250,37 @@ void prim_massvel(double a1, double a2, const double* A, const double* B,
   }, sh);
 }
 
+// Momentum (momentum2CIntg, gaussIntegrals.f90:23041-39068): component c of
+// <a| d/dr_c |b>, the derivative acting on b.  Per direction
+// d/dx [x^l e^{-a2 x^2}] = (l x^{l-1} - 2 a2 x^{l+1}) e^{-a2 x^2}, so the
+// component is a 1-D overlap with b's power lowered or raised by one times
+// the plain overlaps of the other two directions.
+void prim_momentum(double a1, double a2, const double* A, const double* B,
+                   int lma1, int lma2, int comp, double* sh) {
+  const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
+  const double z = a1 + a2, inv2z = 1.0 / (2.0 * z), xi = a1 * a2 / z;
+  double d2 = 0, s[3][8][8];
+  for (int c = 0; c < 3; ++c) {
+    double P = (a1 * A[c] + a2 * B[c]) / z;
+    d2 += (A[c] - B[c]) * (A[c] - B[c]);
+    os_1d(P - A[c], P - B[c], inv2z, l1, l2 + 1, s[c]);
+  }
+  const double pref = std::pow(kPi / z, 1.5) * std::exp(-xi * d2);
+  cart_to_sh(lma1, lma2, [&](const int* ea, const int* eb) {
+    double v = pref;
+    for (int c = 0; c < 3; ++c) {
+      if (c == comp) {
+        double d = -2.0 * a2 * s[c][ea[c]][eb[c] + 1];
+        if (eb[c] > 0) d += eb[c] * s[c][ea[c]][eb[c] - 1];
+        v *= d;
+      } else {
+        v *= s[c][ea[c]][eb[c]];
+      }
+    }
+    return v;
+  }, sh);
+}
+
 void prim_elec3c(double a1, double a2, double a3, const double* A, const double* B,
                  const double* Cc, int lma1, int lma2, double* sh) {
   const int l1 = lmax_of(lma1), l2 = lmax_of(lma2);
@@ -981,7 +1012,7 @@ void orc_ortho_pack(void* h, int is_overlap, double* vv, const double* cv, const
 }
 
 // Primitive evaluation: kind 1 overlap, 2 kinetic, 3 nuclear, 4 electron3C,
-// 5 mass velocity.
+// 5 mass velocity, 6 / 7 / 8 momentum x / y / z.
 // in = (a1,a2,a3,A[3],B[3],C[3]); out = sh(16,16) column-major.
 void orc_primitive(int kind, const double* in, const int32_t* lmalpha, double* out) {
   for (int q = 0; q < 256; ++q) out[q] = 0.0;
@@ -992,6 +1023,9 @@ void orc_primitive(int kind, const double* in, const int32_t* lmalpha, double* o
     case 3: prim_nuclear(in[0], in[1], in[2], A, B, Cc, lmalpha[0], lmalpha[1], out); break;
     case 4: prim_elec3c(in[0], in[1], in[2], A, B, Cc, lmalpha[0], lmalpha[1], out); break;
     case 5: prim_massvel(in[0], in[1], A, B, lmalpha[0], lmalpha[1], out); break;
+    case 6:
+    case 7:
+    case 8: prim_momentum(in[0], in[1], A, B, lmalpha[0], lmalpha[1], kind - 6, out); break;
   }
 }
 

@@ -56,3 +56,26 @@ def test_device_primitives_match_reference(gpu_lib, golden, kind):
         assert e <= tol, f"kind {kind} item {i} lm {lm[i]}: rel err {e:.2e}"
         worst = max(worst, e)
     assert worst < 1e-9
+
+
+@pytest.mark.gpu
+def test_device_momentum_matches_reference(gpu_lib):
+    """momentum2CIntg (kinds 6-8, the x, y, z components) for every class
+    pair s..f against the reference's own blocks (tests/golden/momentum.npz),
+    within the bar of tests/test_momentum.py (1e-11 of the block plus the
+    rounding of the reference's P - A at very unequal exponents)."""
+    import os
+    from olcao_gb300 import api
+    import oracle as orc
+    mom = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "momentum.npz"))
+    params, lm, ref = mom["params"], mom["lmalpha"], mom["sh"]
+    got = [api.primitive_batch(6 + c, params, lm) for c in range(3)]
+    for i in range(len(params)):
+        l1, l2 = (int(x) for x in lm[i])
+        ov = np.abs(orc.primitive(1, params[i], [l1, l2])[:l1, :l2]).max()
+        reach = 1.0 + np.abs(params[i][3:6]).max() + np.abs(params[i][6:9]).max()
+        tol = (1e-11 * np.abs(ref[i][:l1, :l2]).max() +
+               64 * 2.0 ** -52 * reach * 2.0 * max(params[i][0], params[i][1]) * ov)
+        for c in range(3):
+            err = np.abs(got[c][i][:l1, :l2] - ref[i][:l1, :l2, c]).max()
+            assert err <= tol, f"block {i} lm ({l1},{l2}) component {c}: {err:.2e} > {tol:.2e}"
