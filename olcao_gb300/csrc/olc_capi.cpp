@@ -110,24 +110,11 @@ int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
   olc_context* ctx = new olc_context();
   ctx->device = dev;
   ctx->stream = static_cast<cudaStream_t>(stream);
-  if (cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) {
-    delete ctx;
-    return fail(OLC_ERR_CUDA, "cublasCreate failed");
-  }
   if (cusolverDnCreate(&ctx->solver) != CUSOLVER_STATUS_SUCCESS) {
-    cublasDestroy(ctx->blas);
     delete ctx;
     return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
   }
-  cublasSetStream(ctx->blas, ctx->stream);
   cusolverDnSetStream(ctx->solver, ctx->stream);
-  // FP32 products of the mixed solver run as BF16x9 tensor-core emulation
-  // (FP32 accuracy) unless OLC_FP32_GEMM=simt
-  if (cublasCreate(&ctx->blas_f32) != CUBLAS_STATUS_SUCCESS) {
-    olc_destroy(ctx);
-    return fail(OLC_ERR_CUDA, "cublasCreate failed");
-  }
-  cublasSetStream(ctx->blas_f32, ctx->stream);
   {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
@@ -140,13 +127,6 @@ int olc_create(const olc_system_t* sys, void* stream, olc_context_t** out) {
     }
     uint64_t keep = UINT64_MAX;
     cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
-  }
-  {
-    const char* v = std::getenv("OLC_FP32_GEMM");
-    if (!(v && std::string(v) == "simt")) {
-      cublasSetMathMode(ctx->blas_f32, CUBLAS_FP32_EMULATED_BF16X9_MATH);
-      cublasSetEmulationStrategy(ctx->blas_f32, CUBLAS_EMULATION_STRATEGY_EAGER);
-    }
   }
   st = build_system(ctx, sys);
   if (!st) st = build_phase_table(ctx);
@@ -185,8 +165,6 @@ int olc_destroy(olc_context_t* ctx) {
   }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-  if (ctx->blas) cublasDestroy(ctx->blas);
-  if (ctx->blas_f32) cublasDestroy(ctx->blas_f32);
   if (ctx->pool) {
     cudaStreamSynchronize(ctx->stream);
     cudaMemPoolDestroy(ctx->pool);
@@ -205,8 +183,6 @@ int olc_get_dims(const olc_context_t* ctx, olc_dims_t* dims) {
 int olc_set_stream(olc_context_t* ctx, void* stream) {
   if (!ctx) return fail(OLC_ERR_ARG, "olc_set_stream: null context");
   ctx->stream = static_cast<cudaStream_t>(stream);
-  cublasSetStream(ctx->blas, ctx->stream);
-  if (ctx->blas_f32) cublasSetStream(ctx->blas_f32, ctx->stream);
   cusolverDnSetStream(ctx->solver, ctx->stream);
   return OLC_OK;
 }

@@ -3,7 +3,6 @@
 #pragma once
 
 #include <cuda_runtime.h>
-#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <cstdint>
@@ -109,8 +108,6 @@ struct StageEvent {
 struct olc_context {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cublasHandle_t blas = nullptr;
-  cublasHandle_t blas_f32 = nullptr;   // FP32 products (BF16x9 emulation)
   cudaMemPool_t pool = nullptr;        // scratch of the SCF pass, kept between calls
   // CUDA graph of the mixed stored-form pass (OLC_ITER_GRAPH)
   cudaGraphExec_t graph_exec = nullptr;
@@ -279,7 +276,8 @@ int scf_matrices(olc_context* ctx, const double* coeffs, int kpoint, double* h, 
 int scf_iteration(olc_context* ctx, const double* coeffs, int precision, int num_states,
                   double* eigenvalues, int flags, double* vectors);
 
-// FP64-accurate complex products from BF16 tensor-core digits (olc_ozaki.cu):
+// FP64-accurate complex products from BF16 tensor-core digits (olc_ozaki.cu,
+// on the tcgen05 kernel of olc_tcgemm.cu):
 // C[b] = op(A[b]) B[b], A logical m x k (conjA: A = src^H), B k x n, C m x n
 // complex FP64 with batch stride m*n; bits_a/bits_b = bits kept per operand;
 // batch strides sA, sB count elements of TA / TB (two per complex number).
@@ -289,7 +287,6 @@ template <class TA, class TB>
 int ozaki_zgemm(olc_context* ctx, int m, int n, int k, const TA* A, long long sA, int lda,
                 bool conjA, int bits_a, const TB* B, long long sB, int ldb, int bits_b, double* C,
                 int nb, int stage = OLC_STAGE_REFINE, bool hermitian = false);
-void ozaki_plan(int k, int bits_a, int bits_b, int* beta, int* na, int* nbs);
 
 // status of a queued mixed solve (olc_mixed.cu)
 int mixed_check_info(olc_context* ctx);

@@ -8,9 +8,11 @@
 //                    column by column with |x| < 1e-10 flushed when core_dim > 0.
 //   assembly         secularEqn.F90:128-166, matrixSubs.F90:248-355.
 //   solve            solveZHEGV, interfaces.F90:73-120 (itype 1, 'V', 'U').
-// The GEMMs are FP64 complex library GEMMs (cuBLAS); the epilogue that
-// combines, flushes and packs is a hand-written kernel; the small-n solves
-// use a batched in-shared-memory kernel (olc_eigen_small.cu).
+// The orthogonalisation's products are FP64-accurate split-digit products on
+// the tcgen05 kernel (olc_tcgemm.cu, through olc_ozaki.cu); the epilogue that
+// combines, flushes and packs is a hand-written kernel.  The FP64 solve (the
+// reference-equivalent path) uses a batched in-shared-memory kernel for
+// n <= 64 (olc_eigen_small.cu) and cuSOLVER zhegvd per k above.
 #include <cstdlib>
 #include <algorithm>
 #include <cstdio>

@@ -6,12 +6,11 @@
 // FP64-accurate answer is recovered from an FP32 solve instead:
 //
 //   1. FP32 pencil: X (n x n, S-orthonormal to FP32 accuracy) from the
-//      batched FP32 solver of olc_tridiag.cu (all k in one set of launches),
-//      or from cuSOLVER chegvd per k on concurrent streams.
+//      batched FP32 solver of olc_tridiag.cu (all k in one set of launches).
 //   2. Rayleigh-Ritz in that basis with FP64-accurate products:
 //        Hh = X^H (H X),  Sh = X^H (S X),
 //      each formed error-free from BF16 digits on the tensor cores
-//      (olc_ozaki.cu).
+//      (olc_tcgemm.cu fixed mode).
 //   3. Sh = I + E with E ~ 1e-5: the Loewdin transform (I+F)^H Hh (I+F),
 //      F = -E/2 + 3E^2/8, makes the pencil standard to O(E^3); since F is
 //      small its products need only FP32 GEMMs.  The basis becomes X (I+F).
@@ -696,87 +695,7 @@ int loewdin(olc_context* ctx, int n, int nk, double* Hh, double* Sh, float* X) {
   return cuda_check(cudaGetLastError(), "loewdin kernels");
 }
 
-// FP32 eigenvectors by cuSOLVER chegvd, one k per call, the calls spread over
-// host threads and streams (chegvd waits on the device from its host thread).
-// X overwrites h32; s32 is overwritten.
-static int solve_fp32_library(olc_context* ctx, int n, int nk, float* h32, float* s32) {
-  const size_t nn = (size_t)n * n;
-  cudaStream_t stream = ctx->stream;
-  int st;
-  float* w32 = nullptr;
-  if ((st = cuda_check(ctx_malloc(ctx, (void**)&w32, 4 * (size_t)n * nk, stream), "malloc w32"))) return st;
-  const int nsub = std::max(1, std::min(nk, 32));
-  if ((int)ctx->mixed_streams.size() != nsub || ctx->mixed_n != n) {
-    for (size_t i = 0; i < ctx->mixed_streams.size(); ++i) {
-      cudaStreamSynchronize(ctx->mixed_streams[i]);
-      cusolverDnDestroy(ctx->mixed_solvers[i]);
-      cudaFree(ctx->mixed_work[i]);
-      cudaStreamDestroy(ctx->mixed_streams[i]);
-      cudaEventDestroy(ctx->mixed_join[i]);
-    }
-    ctx->mixed_streams.clear(); ctx->mixed_solvers.clear(); ctx->mixed_work.clear();
-    ctx->mixed_join.clear();
-    if (!ctx->ev_fork) cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
-    cusolverDnHandle_t h0;
-    if (cusolverDnCreate(&h0) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
-    int lwork = 0;
-    cusolverStatus_t ss = cusolverDnChegvd_bufferSize(
-        h0, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
-        reinterpret_cast<cuComplex*>(h32), n, reinterpret_cast<cuComplex*>(s32), n, w32, &lwork);
-    cusolverDnDestroy(h0);
-    if (ss != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "chegvd_bufferSize failed");
-    ctx->mixed_lwork = lwork;
-    for (int i = 0; i < nsub; ++i) {
-      cudaStream_t sm;
-      cusolverDnHandle_t hs;
-      void* w = nullptr;
-      cudaEvent_t ej;
-      if ((st = cuda_check(cudaStreamCreateWithFlags(&sm, cudaStreamNonBlocking), "sub stream"))) return st;
-      if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) return fail(OLC_ERR_CUDA, "cusolverDnCreate failed");
-      cusolverDnSetStream(hs, sm);
-      if ((st = cuda_check(cudaMalloc(&w, sizeof(cuComplex) * (size_t)lwork), "chegvd work"))) return st;
-      cudaEventCreateWithFlags(&ej, cudaEventDisableTiming);
-      ctx->mixed_streams.push_back(sm);
-      ctx->mixed_solvers.push_back(hs);
-      ctx->mixed_work.push_back(w);
-      ctx->mixed_join.push_back(ej);
-    }
-    ctx->mixed_n = n;
-  }
-  if (!ctx->d_info && (st = dalloc(ctx, &ctx->d_info, (size_t)nk))) return st;
-  {
-    StageScope scope(ctx, OLC_STAGE_SOLVE, 0);
-    cudaEventRecord(ctx->ev_fork, stream);
-    for (int i = 0; i < nsub; ++i) cudaStreamWaitEvent(ctx->mixed_streams[i], ctx->ev_fork, 0);
-    const float* hbase = h32;
-    st = parallel_host(nsub, ctx->device, [&](int i) -> int {
-      for (int k = i; k < nk; k += nsub) {
-        cusolverStatus_t ss = cusolverDnChegvd(
-            ctx->mixed_solvers[i], CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
-            CUBLAS_FILL_MODE_UPPER, n, reinterpret_cast<cuComplex*>(const_cast<float*>(hbase)) + (size_t)k * nn, n,
-            reinterpret_cast<cuComplex*>(s32) + (size_t)k * nn, n, w32 + (size_t)k * n,
-            reinterpret_cast<cuComplex*>(ctx->mixed_work[i]), ctx->mixed_lwork, ctx->d_info + k);
-        if (ss != CUSOLVER_STATUS_SUCCESS) return OLC_ERR_CUDA;
-      }
-      return 0;
-    });
-    if (st) return fail(st, "cusolverDnChegvd failed");
-    for (int i = 0; i < nsub; ++i) {
-      cudaEventRecord(ctx->mixed_join[i], ctx->mixed_streams[i]);
-      cudaStreamWaitEvent(stream, ctx->mixed_join[i], 0);
-    }
-  }
-  cudaFreeAsync(w32, stream);
-  return OLC_OK;
-}
 
-// The batched FP32 solver is used unless OLC_FP32_SOLVER=library or n is
-// beyond its shared-memory limit.
-static bool use_batched_fp32(int n) {
-  const char* v = std::getenv("OLC_FP32_SOLVER");
-  if (v && std::string(v) == "library") return false;
-  return n >= 2 && n <= hetrd_max_n();
-}
 
 // Solve every k with the mixed-precision scheme; h, s are full Hermitian
 // FP64 [nk][n][n] (not modified).
@@ -791,7 +710,8 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
   // W = U^{-1} (S = U^H U, FP64 factorisation rounded to FP32); the prepared
   // S(k) does not change between passes, so its factors are kept from the
   // first pass
-  const bool batched = use_batched_fp32(n);
+  if (n < 2 || n > hetrd_max_n())
+    return fail(OLC_ERR_UNSUPPORTED, "mixed solver: n outside the batched FP32 solver's range");
   float* h32 = nullptr;
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&h32, 8 * nn * nk, stream), "malloc h32"))) return st;
   {
@@ -799,35 +719,24 @@ int solve_full_mixed(olc_context* ctx, const double* h, const double* s, int num
     to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(h, h32, 2 * nn * nk);
   }
   float* X = nullptr;      // FP32 eigenvectors, [nk][n][n] complex
-  if (batched) {
-    float* w32 = nullptr;
-    if (s_prepared) {
-      if (!ctx->w32 && (st = dalloc(ctx, &ctx->w32, 2 * nn * nk))) return st;
-      w32 = ctx->w32;
-      if (!ctx->w32_valid) {
-        if ((st = inverse_factors(ctx, n, nk, s, w32))) return st;
-        ctx->w32_valid = true;
-      } else if ((st = cuda_check(cudaMemsetAsync(ctx->d_info, 0, sizeof(int) * nk, stream), "clear info"))) {
-        return st;
-      }
-    } else {
-      if ((st = cuda_check(ctx_malloc(ctx, (void**)&w32, 8 * nn * nk, stream), "malloc w32"))) return st;
+  float* w32 = nullptr;
+  if (s_prepared) {
+    if (!ctx->w32 && (st = dalloc(ctx, &ctx->w32, 2 * nn * nk))) return st;
+    w32 = ctx->w32;
+    if (!ctx->w32_valid) {
       if ((st = inverse_factors(ctx, n, nk, s, w32))) return st;
+      ctx->w32_valid = true;
+    } else if ((st = cuda_check(cudaMemsetAsync(ctx->d_info, 0, sizeof(int) * nk, stream), "clear info"))) {
+      return st;
     }
-    if ((st = cuda_check(ctx_malloc(ctx, (void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
-    if ((st = solve_fp32_batched(ctx, n, nk, h32, w32, X))) return st;
-    if (!s_prepared) cudaFreeAsync(w32, stream);
-    cudaFreeAsync(h32, stream);
   } else {
-    float* s32 = nullptr;
-    if ((st = cuda_check(ctx_malloc(ctx, (void**)&s32, 8 * nn * nk, stream), "malloc s32"))) return st;
-    to_c64_kernel<<<grid_for(2 * nn * nk), 256, 0, stream>>>(s, s32, 2 * nn * nk);
-    count_launch();
-    if ((st = solve_fp32_library(ctx, n, nk, h32, s32))) return st;
-    ctx->info_potrf = false;
-    X = h32;
-    cudaFreeAsync(s32, stream);
+    if ((st = cuda_check(ctx_malloc(ctx, (void**)&w32, 8 * nn * nk, stream), "malloc w32"))) return st;
+    if ((st = inverse_factors(ctx, n, nk, s, w32))) return st;
   }
+  if ((st = cuda_check(ctx_malloc(ctx, (void**)&X, 8 * nn * nk, stream), "malloc X"))) return st;
+  if ((st = solve_fp32_batched(ctx, n, nk, h32, w32, X))) return st;
+  if (!s_prepared) cudaFreeAsync(w32, stream);
+  cudaFreeAsync(h32, stream);
   // ---- 2. Rayleigh-Ritz with error-free split products ---------------------
   double *Y = nullptr, *Hh = nullptr, *Sh = nullptr;
   // bits kept of FP64 and FP32 operands (OLC_SPLIT_BITS overrides the FP64 count)
