@@ -233,6 +233,26 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   // segments: every pair over K chunks of chunk_blocks K-blocks
   const int nchunk = (p.kblocks + p.chunk_blocks - 1) / p.chunk_blocks;
   const int nseg = p.npairs * nchunk;
+  // triangular operands (f32 mode): the complex K range [kmin, kmax) this
+  // tile needs; a K-block is issued when it meets that range in the real or
+  // the imaginary half of K' (every role skips the same blocks and segments)
+  int kmin = 0, kmax = p.kp;
+  if (p.tri_a_upper) kmin = m0;
+  if (p.tri_a_lower) kmax = min(kmax, m0 + BM);
+  if (p.tri_b_upper) kmax = min(kmax, (n0 >> 1) + BN / 2);
+  const bool tri = kmin > 0 || kmax < p.kp;
+  auto kb_needed = [&](int kb) {
+    if (!tri) return true;
+    const int lo = kb * BK, hi = lo + BK;
+    return (lo < kmax && hi > kmin) || (lo < p.kp + kmax && hi > p.kp + kmin);
+  };
+  auto seg_live = [&](int si) {
+    if (!tri) return true;
+    const int kb0 = (si % nchunk) * p.chunk_blocks, kb1 = min(p.kblocks, kb0 + p.chunk_blocks);
+    for (int kb = kb0; kb < kb1; ++kb)
+      if (kb_needed(kb)) return true;
+    return false;
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -269,6 +289,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const TcPair pr = p.pairs[si / nchunk];
         const int kb0 = (si % nchunk) * p.chunk_blocks, kb1 = min(p.kblocks, kb0 + p.chunk_blocks);
         for (int kb = kb0; kb < kb1; ++kb) {
+          if (!kb_needed(kb)) continue;
           if (!mbar_wait(&empty[stage], phase ^ 1u, cta_err, p.err, 1)) { ok = false; break; }
           mbar_expect_tx(&full[stage], (uint32_t)(SmemLayout::a_bytes + SmemLayout::b_bytes<BN>()));
           tma_load_3d(sA + stage * SmemLayout::a_bytes, &tmA, &full[stage], kb * BK, m0, b * p.planes_a + pr.pa);
@@ -295,27 +316,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
+      int ls = 0;   // live segments so far (the accumulator ring follows them)
       for (int si = 0; si < nseg && ok; ++si) {
+        if (!seg_live(si)) continue;
         const int kb0 = (si % nchunk) * p.chunk_blocks, kb1 = min(p.kblocks, kb0 + p.chunk_blocks);
-        const int buf = si & 1;
+        const int buf = ls & 1;
         {
-          const uint32_t use = (uint32_t)(si >> 1);
+          const uint32_t use = (uint32_t)(ls >> 1);
           if (!mbar_wait(&accempty[buf], (use & 1u) ^ 1u, cta_err, p.err, 2)) { ok = false; break; }
           tc_fence_after();
         }
+        ++ls;
         const uint32_t dt = tmem + (uint32_t)(buf * BN);
+        bool fresh = true;   // the segment's first issued block overwrites the accumulator
         for (int kb = kb0; kb < kb1; ++kb) {
+          if (!kb_needed(kb)) continue;
           if (!mbar_wait(&full[stage], phase, cta_err, p.err, 3)) { ok = false; break; }
           tc_fence_after();
           const uint64_t ad = sdesc(smem_u32(sA + stage * SmemLayout::a_bytes));
           const uint64_t bd = sdesc(smem_u32(sB + stage * SmemLayout::b_bytes<BN>()));
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {
-            const bool first = kb == kb0 && k == 0;
+            const bool first = fresh && k == 0;
             // +32 bytes of K per instruction: +2 in the descriptor's address field
             umma(dt, ad + 2 * k, bd + 2 * k, IDESC, first ? 0u : 1u);
           }
           umma_commit(&empty[stage]);
+          fresh = false;
           if (++stage == STAGES) { stage = 0; phase ^= 1u; }
         }
         if (ok) umma_commit(&accfull[buf]);
@@ -331,9 +358,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
       for (int j = 0; j < 64; ++j) acc[j] = 0;
       bool ok = true;
+      int ls = 0;
       for (int si = 0; si < nseg; ++si) {
-        const int buf = si & 1;
-        const uint32_t use = (uint32_t)(si >> 1);
+        if (!seg_live(si)) continue;
+        const int buf = ls & 1;
+        const uint32_t use = (uint32_t)(ls >> 1);
+        ++ls;
         ok = __all_sync(0xffffffffu, mbar_wait(&accfull[buf], use & 1u, cta_err, p.err, 4));
         if (!ok) break;
         tc_fence_after();
@@ -386,9 +416,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
       for (int j = 0; j < 128; ++j) acc[j] = 0.f;
       bool ok = true;
+      int ls = 0;
       for (int si = 0; si < nseg; ++si) {
-        const int buf = si & 1;
-        const uint32_t use = (uint32_t)(si >> 1);
+        if (!seg_live(si)) continue;
+        const int buf = ls & 1;
+        const uint32_t use = (uint32_t)(ls >> 1);
+        ++ls;
         ok = __all_sync(0xffffffffu, mbar_wait(&accfull[buf], use & 1u, cta_err, p.err, 4));
         if (!ok) break;
         tc_fence_after();
@@ -689,6 +722,7 @@ int launch(olc_context* ctx, int mode, const void* dA, const void* dB, int plane
   p.nmt = (m + BM - 1) / BM;
   p.nnt = (nreal + BN - 1) / BN;
   p.kblocks = (int)(Kp / BK);
+  p.kp = (int)(Kp / 2);
   p.err = g_err;
   const dim3 grid((unsigned)(p.nmt * p.nnt), (unsigned)nb);
   if (mode == 0) {
@@ -818,7 +852,7 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
 
 int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long sA, int lda, bool conjA,
               const float* B, long long sB, int ldb, float alpha, float beta, float* C, long long sC, int ldc,
-              int nb, int stage, bool lower) {
+              int nb, int stage, bool lower, int tri) {
   cudaStream_t st = ctx->stream;
   const int kp = (k + 31) & ~31;
   const size_t Kp = 2 * (size_t)kp;
@@ -857,6 +891,9 @@ int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long s
     for (int i = 0; i < npairs; ++i) p.pairs[i] = TcPair{pairs[i][0], pairs[i][1], 0};
     p.chunk_blocks = 512 / BK;
     p.lower_only = lower ? 1 : 0;
+    p.tri_a_upper = (tri & kTriAUpper) != 0;
+    p.tri_a_lower = (tri & kTriALower) != 0;
+    p.tri_b_upper = (tri & kTriBUpper) != 0;
     if ((s = launch(ctx, 1, wa, wb, 3, 3, Kp, m, 2 * n, cb, p, stage))) return s;
   }
   cudaFreeAsync(wa, st);

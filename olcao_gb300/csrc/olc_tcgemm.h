@@ -34,6 +34,8 @@ struct TcParams {
   int npairs, kblocks, chunk_blocks;   // segments: pairs x ceil(kblocks / chunk_blocks) K chunks
   int herm_upper;               // Hermitian result: tiles wholly below the diagonal are skipped
   int lower_only;               // f32 mode: tiles wholly above the diagonal are skipped
+  int kp;                       // complex K per half of K' (K' = 2 kp)
+  int tri_a_upper, tri_a_lower, tri_b_upper;   // triangular operands: zero K blocks skipped
   int* err;                     // device error word (expired waits)
   TcPair pairs[kMaxPairs];
 };
@@ -48,13 +50,19 @@ int zgemm_fixed(olc_context* ctx, int m, int n, int k, const TA* A, long long sA
                 const TB* B, long long sB, int ldb, int bits_b, double* C, int nb, int stage,
                 bool hermitian = false);
 
+// Triangular operands of cgemm_f32: op(A) upper triangular (op(A)(r, k) = 0
+// for k < r), op(A) lower triangular (zero for k > r), B upper triangular
+// (B(k, c) = 0 for k > c).  Each output tile then skips the K blocks that
+// meet only zeros.
+constexpr int kTriAUpper = 1, kTriALower = 2, kTriBUpper = 4;
+
 // FP32-accurate complex product C[b] = alpha op(A[b]) B[b] + beta C[b] from
 // three BF16 pieces per FP32 operand (six piece pairs).  lower: only the
 // output tiles that reach the lower triangle (row >= column) are formed; the
-// rest of C keeps its values.
+// rest of C keeps its values.  tri: kTri* flags of triangular operands.
 int cgemm_f32(olc_context* ctx, int m, int n, int k, const float* A, long long sA, int lda, bool conjA,
               const float* B, long long sB, int ldb, float alpha, float beta, float* C, long long sC, int ldc,
-              int nb, int stage, bool lower = false);
+              int nb, int stage, bool lower = false, int tri = 0);
 
 // Digits and kept pairs of a fixed-point product (see olc_tcgemm.cu).
 void fixed_plan(int bits_a, int bits_b, int prec, int* na, int* nbd, int* T);

@@ -1189,11 +1189,14 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, const float* h32, const 
   if ((st = cuda_check(ctx_malloc(ctx, (void**)&T, 8 * n2 * nk, stream), "malloc H W"))) return st;
   if (ld != n && (st = cuda_check(cudaMemsetAsync(C, 0, 8 * nn * nk, stream), "clear padding"))) return st;
   // ---- 1. C = W^H (H W) ------------------------------------------------------
+  // W is upper triangular: H W skips the K blocks below each column, W^H (H W)
+  // those right of each row
   if ((st = tc::cgemm_f32(ctx, n, n, n, h32, 2 * (long long)n2, n, false, w32, 2 * (long long)n2, n, 1.f, 0.f, T,
-                          2 * (long long)n2, n, nk, OLC_STAGE_SOLVE)))
+                          2 * (long long)n2, n, nk, OLC_STAGE_SOLVE, false, tc::kTriBUpper)))
     return st;
   if ((st = tc::cgemm_f32(ctx, n, n, n, w32, 2 * (long long)n2, n, true, T, 2 * (long long)n2, n, 1.f, 0.f,
-                          reinterpret_cast<float*>(C), 2 * (long long)nn, ld, nk, OLC_STAGE_SOLVE)))
+                          reinterpret_cast<float*>(C), 2 * (long long)nn, ld, nk, OLC_STAGE_SOLVE, false,
+                          tc::kTriALower)))
     return st;
   cudaFreeAsync(T, stream);
   float2* H = C;
@@ -1310,7 +1313,8 @@ int solve_fp32_batched(olc_context* ctx, int n, int nk, const float* h32, const 
   }
   // ---- 5. X = W Z ---------------------------------------------------------------
   if ((st = tc::cgemm_f32(ctx, n, n, n, w32, 2 * (long long)n2, n, false, reinterpret_cast<float*>(Xc),
-                          2 * (long long)nn, ld, 1.f, 0.f, X, 2 * (long long)n2, n, nk, OLC_STAGE_BACKTRANSFORM)))
+                          2 * (long long)nn, ld, 1.f, 0.f, X, 2 * (long long)n2, n, nk, OLC_STAGE_BACKTRANSFORM, false,
+                          tc::kTriAUpper)))
     return st;
   cudaFreeAsync(C, stream);
   cudaFreeAsync(Zc, stream);
