@@ -180,6 +180,83 @@ module O_GB300
          real(c_double), intent(in) :: eigenValues(*)
          type(c_ptr), value :: vectors
       end function
+
+      ! library version string (NUL-terminated, static storage)
+      type(c_ptr) function olc_version() bind(C, name="olc_version")
+         import :: c_ptr
+      end function
+      ! work of the context on another CUDA stream (c_null_ptr: legacy stream)
+      integer(c_int) function olc_set_stream(ctx, stream) bind(C, name="olc_set_stream")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx, stream
+      end function
+
+      ! allocation-free solve for n <= 64 from caller-owned DEVICE arrays:
+      ! packedH, packedS (2, n(n+1)/2, nk), eigenValues (numStates, nk),
+      ! vectors (n, numStates, nk) or c_null_ptr, info (nk); no counterpart
+      ! in the reference (see include/olcao_gpu.h for the limits)
+      integer(c_int) function olc_solve_zhegv_noalloc(n, nk, packedH, packedS, numStates, &
+            & eigenValues, vectors, info, stream) bind(C, name="olc_solve_zhegv_noalloc")
+         import :: c_int, c_ptr
+         integer(c_int), value :: n, nk, numStates
+         type(c_ptr), value :: packedH, packedS, eigenValues, vectors, info, stream
+      end function
+
+      ! the tensor-core products the mixed solver uses, on DEVICE arrays
+      ! (column-major): FP64-accurate c = a b and FP32-accurate c = op(a) b
+      integer(c_int) function olc_split_zgemm(ctx, m, n, k, a, b, c) bind(C, name="olc_split_zgemm")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx, a, b, c
+         integer(c_int), value :: m, n, k
+      end function
+      integer(c_int) function olc_split_cgemm32(ctx, m, n, k, a, conjA, b, c) &
+            & bind(C, name="olc_split_cgemm32")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx, a, b, c
+         integer(c_int), value :: m, n, k, conjA
+      end function
+
+      ! the generated primitives (gaussIntegrals.f90) for a batch of explicit
+      ! inputs: kind 1 overlap, 2 kinetic, 3 nuclear, 4 electron 3-centre,
+      ! 5 mass velocity, 6 / 7 / 8 momentum x / y / z; inputs(12, n) =
+      ! (a1, a2, a3, A, B, C), lmAlpha(2, n), sh(16, 16, n) (host arrays)
+      integer(c_int) function olc_primitive_batch(kind, n, inputs, lmAlpha, sh) &
+            & bind(C, name="olc_primitive_batch")
+         import :: c_int, c_double, c_int32_t
+         integer(c_int), value :: kind, n
+         real(c_double), intent(in) :: inputs(*)
+         integer(c_int32_t), intent(in) :: lmAlpha(*)
+         real(c_double), intent(out) :: sh(*)
+      end function
+
+      ! stage timing and work counters (the reference's timeStampStart /
+      ! timeStampEnd around its stages), and the library's kernel count
+      integer(c_int) function olc_profile_enable(ctx, on) bind(C, name="olc_profile_enable")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+         integer(c_int), value :: on
+      end function
+      integer(c_int) function olc_profile_reset(ctx) bind(C, name="olc_profile_reset")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+      end function
+      integer(c_int) function olc_profile_read(ctx, stage, launches, ms) bind(C, name="olc_profile_read")
+         import :: c_int, c_ptr, c_int64_t, c_double
+         type(c_ptr), value :: ctx
+         integer(c_int), value :: stage
+         integer(c_int64_t), intent(out) :: launches
+         real(c_double), intent(out) :: ms
+      end function
+      integer(c_int) function olc_profile_read_work(ctx, stage, flops, bytes) &
+            & bind(C, name="olc_profile_read_work")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: ctx
+         integer(c_int), value :: stage
+         real(c_double), intent(out) :: flops, bytes
+      end function
+      integer(c_int64_t) function olc_launch_count() bind(C, name="olc_launch_count")
+         import :: c_int64_t
+      end function
    end interface
 
 contains

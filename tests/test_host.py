@@ -87,3 +87,17 @@ def test_g_functions_are_refused_by_the_gpu_build(gpu_free_lib):
     with pytest.raises(api.OlcError) as e:
         api.primitive_batch(1, np.zeros((1, 12)) + 1.0, np.array([[25, 1]], np.int32))
     assert e.value.status == 1
+
+
+def test_fortran_binding_covers_every_entry_point():
+    """include/olcao_gpu.f90 (the ISO_C_BINDING module a maintainer adds to
+    the reference's build) binds every entry point include/olcao_gpu.h
+    declares, by the same name."""
+    import os
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "include", "olcao_gpu.h")) as fh:
+        declared = set(re.findall(r"^(?:int|int64_t|const char\*)\s+(olc_\w+)\s*\(", fh.read(), re.M))
+    with open(os.path.join(root, "include", "olcao_gpu.f90")) as fh:
+        bound = set(re.findall(r'bind\s*\(\s*C\s*,\s*name\s*=\s*"(olc_\w+)"', fh.read(), re.I))
+    assert declared and declared == bound, (sorted(declared - bound), sorted(bound - declared))
